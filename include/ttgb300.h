@@ -1,0 +1,164 @@
+/*
+ * ttgb300.h - C ABI of the GB300-native AMEn solver for linear systems in the tensor-train format.
+ *
+ * This is the drop-in boundary for torchTT's AMEn path. It replaces the reference's native entry
+ * point `torchttcpp.amen_solve` (cpp/amen_solve.h:122-139, registered at cpp/cpp_ext.cpp:26) and,
+ * for kernel-level parity, the contraction helpers of cpp/amen_solve.h:17-98.
+ *
+ * Conventions
+ *   - All core pointers are DEVICE pointers to contiguous row-major float64 arrays in the
+ *     reference's layouts: TT-matrix cores r x m x n x r', TT-vector cores r x n x r'
+ *     (torchtt/_tt_base.py:138-145). Inputs are borrowed; nothing is written through them.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream). All work is ordered on it.
+ *   - Every function returns a status code (TTGB_OK = 0); ttgb_last_error() returns the message of
+ *     the last failure on the calling thread. No function throws or aborts.
+ *   - Solutions are library-owned until ttgb_solution_free().
+ *   - There is no CPU fallback: without a CUDA device every entry point returns TTGB_ERR_CUDA.
+ */
+#ifndef TTGB300_H
+#define TTGB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TTGB_OK 0
+#define TTGB_ERR_INVALID 1      /* shape / rank / argument errors (torchtt/errors.py:4-29) */
+#define TTGB_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define TTGB_ERR_NUMERICAL 3    /* NaN/Inf or an unrecoverable breakdown */
+#define TTGB_NOT_CONVERGED 4    /* informational, not returned as an error */
+#define TTGB_ERR_OOM 5
+#define TTGB_ERR_TIMEOUT 6
+#define TTGB_ERR_INTERNAL 7
+
+#define TTGB_PREC_NONE 0        /* preconditioner=None  (torchtt/solvers.py:275-282) */
+#define TTGB_PREC_C 1           /* preconditioner='c'   (cpp/matvecs.h:161-165) */
+#define TTGB_PREC_R 2           /* preconditioner='r'   (cpp/matvecs.h:166-174) */
+
+/* A TT-matrix (rows != NULL) or TT-vector (rows == NULL) of d cores. */
+typedef struct ttgb_tt {
+  int32_t d;
+  const int64_t* rows;          /* M_k, d entries (TT-matrix only) */
+  const int64_t* cols;          /* N_k, d entries */
+  const int64_t* ranks;         /* d + 1 entries, ranks[0] = ranks[d] = 1 */
+  const double* const* cores;   /* d device pointers */
+} ttgb_tt;
+
+/* Parameters of torchttcpp.amen_solve (cpp/amen_solve.h:130-139), same meaning and defaults
+ * (torchtt/solvers.py:211): nswp 22, eps 1e-10, rmax 32768, max_full 500, kickrank 4, kick2 0,
+ * local_iterations 40, resets 2, verbose 0, preconditioner TTGB_PREC_NONE. `seed` drives the
+ * counter-based RNG of the enrichment cores when no z0 is given. */
+typedef struct ttgb_amen_params {
+  int32_t nswp;
+  double eps;
+  int64_t rmax;
+  int64_t max_full;
+  int32_t kickrank;
+  int32_t kick2;
+  int32_t local_iterations;
+  int32_t resets;
+  int32_t verbose;
+  int32_t preconditioner;
+  uint64_t seed;
+  int32_t profile;              /* 1: time the contraction launches with CUDA events (stats) */
+} ttgb_amen_params;
+
+/* Per-solve statistics. */
+typedef struct ttgb_stats {
+  int32_t sweeps;
+  int32_t converged;            /* 1 when the max local residual fell below eps (last sweep run) */
+  double max_res;               /* max local residual of the final sweep (amen_solve.h:375) */
+  int64_t local_solves;
+  int64_t direct_solves;
+  int64_t gmres_iterations;
+  int64_t matvecs;              /* local products of the projected system */
+  double matvec_flops;          /* algorithmic flops of those products: 2 r n R (r s + n s S + R S) */
+  double phi_flops;             /* algorithmic flops of the interface updates */
+  double other_flops;           /* enrichment / z products */
+  int64_t host_syncs;
+  double contract_ms;           /* profile only: device time of the contraction kernels */
+  int64_t contract_launches;    /* profile only: number of contraction kernel launches */
+  double contract_flops;        /* profile only: algorithmic flops of those launches */
+} ttgb_stats;
+
+typedef struct ttgb_solution ttgb_solution;   /* opaque, library-owned result */
+
+/* Fills `p` with the reference defaults. */
+void ttgb_default_params(ttgb_amen_params* p);
+
+/* AMEn solve of A x = b (replaces torchttcpp.amen_solve, cpp/amen_solve.h:122-549).
+ * x0 may be NULL or have d == 0 (start from the all-ones tensor, amen_solve.h:161-163).
+ * z0 may be NULL (enrichment cores drawn from the seeded RNG) or give the d initial enrichment
+ * cores of ranks [1, kickrank+kick2, ..., 1] (the reference draws them with torch::randn,
+ * amen_solve.h:174-176). On success *out receives the solution. */
+int ttgb_amen_solve(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, const ttgb_tt* z0,
+                    const ttgb_amen_params* params, void* stream, ttgb_solution** out);
+
+/* Solution accessors. ranks must hold d + 1 entries. */
+int ttgb_solution_dims(const ttgb_solution* sol, int32_t* d, int64_t* ranks);
+int ttgb_solution_stats(const ttgb_solution* sol, ttgb_stats* stats);
+/* Device pointer of core k (r_k x n_k x r_{k+1}, row-major), valid until ttgb_solution_free. */
+const double* ttgb_solution_core(const ttgb_solution* sol, int32_t k);
+/* Copies core k to dst (host memory when dst_is_host != 0, else device memory). */
+int ttgb_solution_copy_core(const ttgb_solution* sol, int32_t k, double* dst, int32_t dst_is_host,
+                            void* stream);
+void ttgb_solution_free(ttgb_solution* sol);
+
+/* ---- kernel-level entry points (FP64, device pointers, workspace allocated internally) ---- */
+
+/* y[l,m,L] = sum Phi_l[l,s,r] A[s,m,n,S] Phi_r[L,S,R] x[r,n,R]
+ * (replaces local_product, cpp/amen_solve.h:17-27, and AMENsolveMV::matvec, cpp/matvecs.h:196-212).
+ * nrhs > 1 applies the operator to nrhs stacked inputs x (stride r*n*R) into y (stride rl*m*RL). */
+int ttgb_local_product(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, int64_t S,
+                       int64_t RL, int64_t R, const double* phi_l, const double* A,
+                       const double* phi_r, const double* x, double* y, int32_t nrhs, void* stream);
+
+/* Interface updates (replace compute_phi_fwd_A / compute_phi_bck_A / compute_phi_fwd_rhs /
+ * compute_phi_bck_rhs, cpp/amen_solve.h:58-68, 38-47, 93-98, 78-83).
+ *   fwd_A: phi[l,s,r], left[l,M,L], A[s,M,N,S], right[r,N,R] -> out[L,S,R]
+ *   bck_A: phi[L,S,R], left[l,M,L], A[s,M,N,S], right[r,N,R] -> out[l,s,r]        */
+int ttgb_phi_fwd_A(int64_t l, int64_t L, int64_t s, int64_t S, int64_t r, int64_t R, int64_t M,
+                   int64_t N, const double* phi, const double* left, const double* A,
+                   const double* right, double* out, void* stream);
+int ttgb_phi_bck_A(int64_t l, int64_t L, int64_t s, int64_t S, int64_t r, int64_t R, int64_t M,
+                   int64_t N, const double* phi, const double* left, const double* A,
+                   const double* right, double* out, void* stream);
+/*   fwd_rhs: phi[b,r], core_b[b,n,B], core[r,n,R] -> out[B,R]
+ *   bck_rhs: phi[B,R], core_b[b,n,B], core[r,n,R] -> out[b,r]                        */
+int ttgb_phi_fwd_rhs(int64_t b, int64_t B, int64_t r, int64_t R, int64_t n, const double* phi,
+                     const double* core_b, const double* core, double* out, void* stream);
+int ttgb_phi_bck_rhs(int64_t b, int64_t B, int64_t r, int64_t R, int64_t n, const double* phi,
+                     const double* core_b, const double* core, double* out, void* stream);
+
+/* Thin QR of the column-major m x n matrix a (lda): q (m x k), r (k x n), k = min(m, n)
+ * (replaces at::linalg_qr at cpp/amen_solve.h:242,254,437,454 and cpp/ortho.h:59). */
+int ttgb_qr(const double* a, int64_t lda, int64_t m, int64_t n, double* q, double* r, void* stream);
+/* Thin SVD of the column-major m x n matrix a: u (m x k), s (k, descending), vh (k x n)
+ * (replaces at::linalg_svd(.., false) at cpp/amen_solve.h:231,383,430). */
+int ttgb_svd(const double* a, int64_t lda, int64_t m, int64_t n, double* u, double* s, double* vh,
+             void* stream);
+
+/* Solves the local system Phi_l x A x Phi_r (x) = rhs with the restarted GMRES of the AMEn local
+ * step (replaces gmres, cpp/gmres.h:146-161, on AMENsolveMV): x starts at 0, `threshold` is the
+ * relative residual target, at most `iters` iterations per cycle and `resets` cycles. The
+ * preconditioned variable is mapped back when `prec` != 0. Returns flag/iteration count. */
+int ttgb_local_gmres(int64_t r, int64_t s, int64_t n, int64_t S, int64_t R, const double* phi_l,
+                     const double* A, const double* phi_r, const double* rhs, double* x,
+                     int32_t iters, double threshold, int32_t resets, int32_t prec,
+                     int32_t* flag, int32_t* nit, void* stream);
+
+/* Number of kernels this library has launched in the process so far. */
+int64_t ttgb_launch_count(void);
+
+/* Message of the last error on this thread. */
+const char* ttgb_last_error(void);
+/* ABI version: 100 * major + minor. */
+int32_t ttgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TTGB300_H */

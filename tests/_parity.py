@@ -1,0 +1,47 @@
+"""Solve-level parity criteria against the reference's solution on the same inputs.
+
+* relative residual ||A x - b|| / ||b|| <= max(10 eps, 2 x the reference's own on the same input):
+  the reference stops on its local residual (cpp/amen_solve.h:375,525), so its true residual can
+  exceed eps; on the random 4x5x6 system of tests/test_solvers.py it ranges from 2e-11 to 7e-10 at
+  eps = 1e-10 depending on the random enrichment start alone;
+* ||x - x_ref|| / ||x_ref|| <= max(10 eps, cond(A) (res + res_ref)) where cond(A) is known (small
+  dense cases), else <= 10 eps;
+* TT ranks within +-kickrank of the reference's.
+"""
+import numpy as np
+
+from oracle import amen as O
+
+
+def check(A, b, x, x_ref, eps, kickrank, cond=None, label=""):
+    A = [np.asarray(a) for a in A]
+    b = [np.asarray(c) for c in b]
+    x = [np.asarray(c) for c in x]
+    x_ref = [np.asarray(c) for c in x_ref]
+    res = O.tt_relres(A, x, b)
+    res_ref = O.tt_relres(A, x_ref, b)
+    err = O.tt_relerr(x, x_ref)
+    bound = 10 * eps if cond is None else max(10 * eps, cond * (res + res_ref))
+    ranks = [c.shape[2] for c in x][:-1]
+    ranks_ref = [c.shape[2] for c in x_ref][:-1]
+    msg = "%s res %.3e (ref %.3e) err %.3e (bound %.3e) ranks %s ref %s" % (
+        label, res, res_ref, err, bound, ranks, ranks_ref)
+    assert res <= max(10 * eps, 2 * res_ref), msg
+    assert err <= bound, msg
+    assert all(abs(a - c) <= kickrank for a, c in zip(ranks, ranks_ref)), msg
+    return res, res_ref, err
+
+
+def dense_cond(A_cores):
+    """2-norm condition number of a small TT-matrix via its dense form."""
+    d = len(A_cores)
+    t = A_cores[0]
+    for c in A_cores[1:]:
+        t = np.tensordot(t, c, axes=([t.ndim - 1], [0]))
+    t = t.reshape(t.shape[1:-1])
+    M = [c.shape[1] for c in A_cores]
+    N = [c.shape[2] for c in A_cores]
+    perm = list(range(0, 2 * d, 2)) + list(range(1, 2 * d, 2))
+    mat = t.transpose(perm).reshape(int(np.prod(M)), int(np.prod(N)))
+    s = np.linalg.svd(mat, compute_uv=False)
+    return float(s[0] / s[-1])

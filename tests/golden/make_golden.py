@@ -1,0 +1,155 @@
+"""Generate the golden fixtures of the AMEn path from the reference itself.
+
+Runs where the reference tree is present (it is read from ``$TORCHTT_REFERENCE``, default
+``/root/reference``): the reference's C++ extension is compiled by ``oracle/build_ref.py`` and its
+Python package is imported from the tree. Writes ``tests/golden/*.npz``:
+
+* ``kernels.npz`` - inputs and outputs of the reference's local product and the four interface
+  updates (``torchtt/solvers.py:36-68,691-775``, the Python twins of ``cpp/amen_solve.h:17-98``) on
+  seeded random shapes, plus a GMRES known answer (``torchtt/_iterative_solvers.py:72-158`` on a
+  1-D Laplacian, the pattern of ``cpp/test_gmres.cpp:187-253``);
+* ``solve_<name>.npz`` - the inputs of a whole solve (A, b, x0 cores, the initial enrichment cores z0
+  that the reference drew with ``torch::randn`` after ``torch.manual_seed``), the parameters, and the
+  solution cores returned by ``torchttcpp.amen_solve`` (``cpp/amen_solve.h:122``) and, for the small
+  cases, by the Python path ``_amen_solve_python`` (``torchtt/solvers.py:290``).
+
+Usage: ``python tests/golden/make_golden.py``
+"""
+import os
+import sys
+import time
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import build_ref  # noqa: E402
+from torchtt_gb300 import workloads as W  # noqa: E402
+
+
+def _pack_cores(prefix, cores, out):
+    out[prefix + "_n"] = np.array(len(cores))
+    for i, c in enumerate(cores):
+        out["%s_%d" % (prefix, i)] = np.ascontiguousarray(c.numpy() if torch.is_tensor(c) else c)
+
+
+def kernels(torchtt):
+    from torchtt import solvers as S
+    from torchtt import _iterative_solvers as IS
+    g = np.random.Generator(np.random.PCG64(7))
+    out = {}
+    cases = [(3, 5, 4, 2, 3), (7, 6, 9, 3, 2), (12, 16, 10, 2, 2), (1, 8, 5, 1, 3)]
+    for ci, (r, n, R, s, S_) in enumerate(cases):
+        PhiL = g.standard_normal((r, s, r))
+        PhiR = g.standard_normal((R, S_, R))
+        Ak = g.standard_normal((s, n, n, S_))
+        x = g.standard_normal((r, n, R))
+        t = lambda a: torch.from_numpy(a)
+        y = S._local_product(t(PhiR), t(PhiL), t(Ak), t(x), x.shape)
+        # interface updates: x core of shape r x n x R, z core rz x n x Rz
+        rz, Rz = max(1, r // 2), max(1, R // 2)
+        z = g.standard_normal((rz, n, Rz))
+        Pf = g.standard_normal((rz, s, r))          # Phi for (z, x): rz x s x r
+        Pb = g.standard_normal((Rz, S_, R))
+        rb, Rb = 2, 3
+        bk = g.standard_normal((rb, n, Rb))
+        Pbf = g.standard_normal((rb, r))
+        Pbb = g.standard_normal((Rb, R))
+        fwdA = S._compute_phi_fwd_A(t(Pf), t(z), t(Ak), t(x))
+        bckA = S._compute_phi_bck_A(t(Pb), t(z), t(Ak), t(x))
+        fwdb = S._compute_phi_fwd_rhs(t(Pbf), t(bk), t(x))
+        bckb = S._compute_phi_bck_rhs(t(Pbb), t(bk), t(x))
+        for k, v in dict(PhiL=PhiL, PhiR=PhiR, A=Ak, x=x, y=y.numpy(), z=z, Pf=Pf, Pb=Pb, bk=bk,
+                         Pbf=Pbf, Pbb=Pbb, fwdA=fwdA.numpy(), bckA=bckA.numpy(),
+                         fwdb=fwdb.numpy(), bckb=bckb.numpy()).items():
+            out["c%d_%s" % (ci, k)] = np.ascontiguousarray(v)
+    out["ncases"] = np.array(len(cases))
+
+    # GMRES known answer on the 1-D Laplacian (-1 2 -1), rhs = ones with zero ends
+    n = 200
+    L = 2 * np.eye(n) - np.eye(n, k=1) - np.eye(n, k=-1)
+
+    class Op:
+        def matvec(self, v):
+            return torch.reshape(torch.from_numpy(L) @ torch.reshape(v, [-1, 1]), [-1, 1])
+    rhs = np.ones((n, 1))
+    rhs[0, 0] = rhs[-1, 0] = 0.0
+    xg, flag, nit = IS.gmres_restart(Op(), torch.from_numpy(rhs), torch.zeros((n, 1), dtype=torch.float64),
+                                     n, 40, 1e-10, 4)
+    out["gmres_L"] = L
+    out["gmres_rhs"] = rhs[:, 0]
+    out["gmres_x"] = xg.numpy()[:, 0]
+    out["gmres_flag"] = np.array(int(flag))
+    out["gmres_nit"] = np.array(int(nit))
+    np.savez_compressed(os.path.join(HERE, "kernels.npz"), **out)
+    print("kernels.npz written")
+
+
+def solve_case(torchtt, cpp, wl, seed, prec=None, with_python=False, extra=None):
+    A, b, x0 = wl["A"], wl["b"], wl.get("x0")
+    p = dict(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
+             local_iterations=40, resets=2)
+    p.update(wl["params"])
+    if extra:
+        p.update(extra)
+    d = len(A)
+    N = [c.shape[2] for c in A]
+    rA = [1] + [c.shape[3] for c in A]
+    rb = [1] + [c.shape[2] for c in b]
+    x_cores = list(x0) if x0 is not None else []
+    rx = ([1] + [c.shape[2] for c in x0]) if x0 is not None else [1] * (d + 1)
+    precode = {None: 0, "c": 1, "r": 2}[prec]
+    torch.manual_seed(seed)
+    rz = [1] + [p["kickrank"] + p["kick2"]] * (d - 1) + [1]
+    z0 = [torch.randn(rz[i], N[i], rz[i + 1], dtype=torch.float64) for i in range(d)]
+    torch.manual_seed(seed)
+    t0 = time.time()
+    xr = cpp.amen_solve(A, b, x_cores, N, rA, rb, rx, p["nswp"], p["eps"], p["rmax"], p["max_full"],
+                        p["kickrank"], p["kick2"], p["local_iterations"], p["resets"], False, precode)
+    t_cpp = time.time() - t0
+    out = {}
+    _pack_cores("A", A, out)
+    _pack_cores("b", b, out)
+    if x0 is not None:
+        _pack_cores("x0", x0, out)
+    _pack_cores("z0", z0, out)
+    _pack_cores("x_cpp", xr, out)
+    for k, v in p.items():
+        out["p_" + k] = np.array(v)
+    out["prec"] = np.array(precode)
+    out["seed"] = np.array(seed)
+    out["t_cpp"] = np.array(t_cpp)
+    out["threads"] = np.array(torch.get_num_threads())
+    if with_python:
+        from torchtt import solvers as S
+        torch.manual_seed(seed)
+        x0tt = torchtt.TT(list(x0)) if x0 is not None else None
+        xp = S.amen_solve(torchtt.TT(list(A)), torchtt.TT(list(b)), nswp=p["nswp"], x0=x0tt, eps=p["eps"],
+                          kickrank=p["kickrank"], preconditioner=prec, use_cpp=False)
+        _pack_cores("x_py", xp.cores, out)
+    name = wl["name"] + ("" if prec is None else "_prec_" + prec)
+    np.savez_compressed(os.path.join(HERE, "solve_%s.npz" % name), **out)
+    print("solve_%s.npz written (cpp %.2fs)" % (name, t_cpp))
+
+
+def main():
+    torch.set_num_threads(max(1, os.cpu_count() or 1))
+    torchtt, cpp = build_ref.load_reference_package()
+    kernels(torchtt)
+    small = W.small_random_system(0)
+    for prec in (None, "c", "r"):
+        solve_case(torchtt, cpp, small, seed=11, prec=prec, with_python=True,
+                   extra=dict(nswp=40) if prec == "r" else None)
+    solve_case(torchtt, cpp, W.laplace_d8_n16(1), seed=1, with_python=False)
+    # a mid-size Laplacian with a direct-solver end core and GMRES interior cores
+    lap = dict(name="laplace_d5_n12", A=W.laplace_ttm(5, 12),
+               b=W.random_tt([12] * 5, [1, 3, 3, 3, 3, 1], 5), x0=None,
+               params=dict(eps=1e-9, nswp=20, kickrank=4))
+    solve_case(torchtt, cpp, lap, seed=5, with_python=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,76 @@
+"""Solve-level parity of the GPU AMEn path against the reference's own solutions on identical inputs
+(tests/golden/solve_*.npz: same A, b, x0 and the same initial enrichment cores z0), and the
+reference's own solver tests (tests/test_solvers.py:13-65) rerun through the gb300 backend."""
+import numpy as np
+import pytest
+import torch
+
+import _golden as G
+import _parity
+
+pytestmark = pytest.mark.gpu
+
+
+def to_dev(cores, dev):
+    return [torch.from_numpy(np.ascontiguousarray(c)).to(dev) for c in cores]
+
+
+@pytest.mark.parametrize("fixture", G.solve_fixtures())
+def test_solve_matches_reference(cuda, fixture):
+    from torchtt_gb300 import TT, amen_solve
+    z = G.load(fixture)
+    A, b = G.cores(z, "A"), G.cores(z, "b")
+    x0, z0 = G.cores(z, "x0"), G.cores(z, "z0")
+    p = G.params(z)
+    prec = {0: None, 1: "c", 2: "r"}[int(z["prec"])]
+    x, st = amen_solve(TT(to_dev(A, cuda)), TT(to_dev(b, cuda)), nswp=p["nswp"],
+                       x0=TT(to_dev(x0, cuda)) if x0 is not None else None, eps=p["eps"],
+                       rmax=p["rmax"], max_full=p["max_full"], kickrank=p["kickrank"],
+                       kick2=p["kick2"], local_iterations=p["local_iterations"], resets=p["resets"],
+                       preconditioner=prec, z0=to_dev(z0, cuda), return_stats=True)
+    xs = [c.cpu().numpy() for c in x.cores]
+    cond = _parity.dense_cond(A) if int(np.prod([a.shape[1] for a in A])) <= 2000 else None
+    _parity.check(A, b, xs, G.cores(z, "x_cpp"), p["eps"], p["kickrank"], cond=cond, label=fixture)
+    assert st["sweeps"] >= 1 and st["matvecs"] > 0
+
+
+@pytest.mark.parametrize("prec", [None, "c", "r"])
+def test_reference_solver_tests(cuda, prec):
+    """tests/test_solvers.py of the reference: random 4x5x6 TT-matrix, b = A x, eps 1e-10,
+    relative residual < 5e-8 (nswp 40 for 'r' as in its Python variant)."""
+    from torchtt_gb300 import TT, amen_solve, workloads as W
+    for seed in range(3):
+        wl = W.small_random_system(100 + seed)
+        A, b = TT([c.to(cuda) for c in wl["A"]]), TT([c.to(cuda) for c in wl["b"]])
+        xx = amen_solve(A, b, eps=1e-10, preconditioner=prec, nswp=40 if prec == "r" else 22,
+                        seed=seed + 1)
+        err = float((A @ xx - b).norm() / b.norm())
+        assert err < 5e-8, (prec, seed, err)
+
+
+def test_cpu_inputs_roundtrip(cuda):
+    """CPU TT in, CPU TT out (the host-buffer path), same answer as device inputs."""
+    from torchtt_gb300 import TT, amen_solve, workloads as W
+    wl = W.small_random_system(7)
+    A, b = TT(wl["A"]), TT(wl["b"])
+    x_cpu = amen_solve(A, b, seed=3)
+    assert x_cpu.cores[0].device.type == "cpu"
+    x_gpu = amen_solve(A.cuda(), b.cuda(), seed=3)
+    for c1, c2 in zip(x_cpu.cores, x_gpu.cores):
+        assert torch.allclose(c1, c2.cpu(), rtol=0, atol=1e-12 * float(c2.abs().max()))
+
+
+def test_edge_cases(cuda):
+    from torchtt_gb300 import TT, amen_solve, workloads as W
+    # d = 1 (a single dense local solve) and d = 2
+    for d, n in ((1, 12), (2, 9)):
+        A = TT([c.to(cuda) for c in W.laplace_ttm(d, n)])
+        b = TT([c.to(cuda) for c in W.random_tt([n] * d, [1] + [2] * (d - 1) + [1], 5)])
+        x = amen_solve(A, b, eps=1e-10)
+        assert float((A @ x - b).norm() / b.norm()) < 1e-8
+    # rank-1 right-hand side and an x0 of higher rank than needed
+    A = TT([c.to(cuda) for c in W.laplace_ttm(4, 10)])
+    b = TT([c.to(cuda) for c in W.random_tt([10] * 4, [1, 1, 1, 1, 1], 9)])
+    x0 = TT([c.to(cuda) for c in W.random_tt([10] * 4, [1, 6, 6, 6, 1], 10)])
+    x = amen_solve(A, b, x0=x0, eps=1e-9)
+    assert float((A @ x - b).norm() / b.norm()) < 1e-7

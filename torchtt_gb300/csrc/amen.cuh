@@ -1,0 +1,67 @@
+// AMEn solve in the TT format, orchestrated on the host with all tensors device resident
+// (reference: amen_solve, cpp/amen_solve.h:122-549).
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace ttgb {
+
+struct AmenParams {
+  int nswp = 22;
+  double eps = 1e-10;
+  int64_t rmax = 32768;
+  int64_t max_full = 500;
+  int kickrank = 4;
+  int kick2 = 0;
+  int local_iterations = 40;
+  int resets = 2;
+  int verbose = 0;
+  int prec = 0;
+  uint64_t seed = 1;
+  int profile = 0;   // time every local product / interface update with CUDA events
+};
+
+// A TT-matrix or TT-vector given by device pointers (borrowed).
+struct TTView {
+  int d = 0;
+  std::vector<int64_t> rows;    // M_k (TT-matrix only)
+  std::vector<int64_t> cols;    // N_k
+  std::vector<int64_t> ranks;   // d + 1
+  std::vector<const double*> cores;
+};
+
+struct AmenStats {
+  int sweeps = 0;
+  double max_res = 0.0;
+  int64_t local_solves = 0;
+  int64_t gmres_iterations = 0;
+  int64_t matvecs = 0;            // local products of the main system
+  double matvec_flops = 0.0;      // algorithmic FP64 flops of those products
+  double phi_flops = 0.0;         // interface updates (x and z)
+  double other_flops = 0.0;       // z / enrichment products
+  int64_t direct_solves = 0;
+  int64_t host_syncs = 0;
+  int converged = 0;
+  // filled when AmenParams::profile is set: CUDA-event time of the contraction launches
+  double contract_ms = 0.0;
+  int64_t contract_launches = 0;
+  double contract_flops = 0.0;
+};
+
+struct AmenResult {
+  std::vector<DTensor> cores;
+  std::vector<int64_t> ranks;
+  AmenStats stats;
+};
+
+// Solves A x = b. `x0` may have d == 0 (start from the all-ones tensor, amen_solve.h:161-166);
+// `z0` may have d == 0 (draw the enrichment cores from a counter-based RNG seeded by p.seed).
+AmenResult amen_solve(const TTView& A, const TTView& b, const TTView& x0, const TTView& z0,
+                      const AmenParams& p, cudaStream_t stream);
+
+// device RNG: out[i] ~ N(0,1) from (seed, offset + i)
+void randn(double* out, int64_t n, uint64_t seed, uint64_t offset, cudaStream_t s);
+
+}  // namespace ttgb

@@ -1,0 +1,359 @@
+// Vector kernels: two-stage deterministic reductions and element-wise updates (FP64).
+#include <atomic>
+
+#include "blas1.cuh"
+
+namespace ttgb {
+
+static std::atomic<int64_t> g_launches{0};
+int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace {
+
+constexpr int RT = 256;   // threads per reduction block
+constexpr int KC = 8;     // vectors per multi-dot chunk
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block-wide sum of one value per thread; result valid in thread 0
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// Called by every block after writing its partials: the last block sums them in block order.
+// post: 0 = plain sums, 1 = sqrt of vector 0.
+__device__ void last_block_reduce(double* partial, unsigned* counter, int G, int nvec, double* out,
+                                  int post) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = atomicAdd(counter, 1u);
+    is_last = (t == (unsigned)G - 1);
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  for (int v = threadIdx.x; v < nvec; v += blockDim.x) {
+    double s = 0.0;
+    const volatile double* p = partial + (int64_t)v * G;
+    for (int b = 0; b < G; ++b) s += p[b];
+    out[v] = (post == 1 && v == 0) ? sqrt(s) : s;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+__global__ void __launch_bounds__(RT) nrm2_kernel(const double* __restrict__ x, int64_t n,
+                                                   int64_t chunk, double* partial, unsigned* counter,
+                                                   double* out, int post) {
+  __shared__ double sh[32];
+  const int64_t beg = blockIdx.x * chunk, end = min(n, beg + chunk);
+  double s = 0.0;
+  for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
+    const double v = x[i];
+    s = fma(v, v, s);
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  last_block_reduce(partial, counter, gridDim.x, 1, out, post);
+}
+
+__global__ void __launch_bounds__(RT) dot_kernel(const double* __restrict__ x,
+                                                  const double* __restrict__ y, int64_t n,
+                                                  int64_t chunk, double* partial, unsigned* counter,
+                                                  double* out) {
+  __shared__ double sh[32];
+  const int64_t beg = blockIdx.x * chunk, end = min(n, beg + chunk);
+  double s = 0.0;
+  for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) s = fma(x[i], y[i], s);
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  last_block_reduce(partial, counter, gridDim.x, 1, out, 0);
+}
+
+// partial dots of Q_i . q over this block's element range, for all i < k
+__device__ void block_multidot(const double* __restrict__ Q, int64_t ldq, int k,
+                               const double* q, int64_t beg, int64_t end, double* partial, int G,
+                               double* sh) {
+  for (int c0 = 0; c0 < k; c0 += KC) {
+    double acc[KC];
+#pragma unroll
+    for (int j = 0; j < KC; ++j) acc[j] = 0.0;
+    const int nc = min(KC, k - c0);
+    for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
+      const double qv = q[i];
+#pragma unroll
+      for (int j = 0; j < KC; ++j)
+        if (j < nc) acc[j] = fma(Q[(int64_t)(c0 + j) * ldq + i], qv, acc[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < KC; ++j) {
+      if (j < nc) {
+        const double s = block_sum(acc[j], sh);
+        if (threadIdx.x == 0) partial[(int64_t)(c0 + j) * G + blockIdx.x] = s;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(RT) multidot_kernel(const double* __restrict__ Q, int64_t ldq,
+                                                       int k, const double* __restrict__ q,
+                                                       int64_t n, int64_t chunk, double* partial,
+                                                       unsigned* counter, double* out) {
+  __shared__ double sh[32];
+  const int64_t beg = blockIdx.x * chunk, end = min(n, beg + chunk);
+  block_multidot(Q, ldq, k, q, beg, end, partial, gridDim.x, sh);
+  last_block_reduce(partial, counter, gridDim.x, k, out, 0);
+}
+
+__global__ void __launch_bounds__(RT) gs_update_kernel(const double* __restrict__ Q, int64_t ldq,
+                                                        int k, const double* __restrict__ h,
+                                                        double* q, int64_t n, int64_t chunk,
+                                                        double* partial, unsigned* counter,
+                                                        double* out, int dots, int sq) {
+  __shared__ double sh[32];
+  __shared__ double hs[256];
+  const int64_t beg = blockIdx.x * chunk, end = min(n, beg + chunk);
+  double ss = 0.0;
+  for (int c0 = 0; c0 < k || (c0 == 0 && k == 0); c0 += 256) {
+    const int nc = min(256, k - c0);
+    __syncthreads();
+    for (int j = threadIdx.x; j < nc; j += blockDim.x) hs[j] = h[c0 + j];
+    __syncthreads();
+    const bool lastc = c0 + 256 >= k;
+    for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
+      double v = q[i];
+      for (int j = 0; j < nc; ++j) v = fma(-hs[j], Q[(int64_t)(c0 + j) * ldq + i], v);
+      q[i] = v;
+      if (lastc) ss = fma(v, v, ss);
+    }
+    if (k == 0) break;
+  }
+  int nvec = 0;
+  if (dots) {
+    __syncthreads();
+    block_multidot(Q, ldq, k, q, beg, end, partial, gridDim.x, sh);
+    nvec = k;
+  }
+  if (sq) {
+    ss = block_sum(ss, sh);
+    if (threadIdx.x == 0) partial[(int64_t)nvec * gridDim.x + blockIdx.x] = ss;
+    nvec += 1;
+  }
+  last_block_reduce(partial, counter, gridDim.x, nvec, out, 0);
+}
+
+__global__ void axpby_kernel(double a, const double* __restrict__ x, double b, double* y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (b == 0.0) ? a * x[i] : fma(a, x[i], b * y[i]);
+}
+
+__global__ void sub_kernel(const double* __restrict__ x, const double* __restrict__ y, double* z,
+                           int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = x[i] - y[i];
+}
+
+__global__ void scale_dev_kernel(double* x, int64_t n, const double* num, const double* den) {
+  const double d = *den;
+  if (!(d > 0.0)) return;
+  const double f = (num ? *num : 1.0) / d;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] *= f;
+}
+
+__global__ void scale_copy_kernel(const double* __restrict__ x, double a, double* y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i];
+}
+
+__global__ void fill_kernel(double* x, double v, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = v;
+}
+
+__global__ void copy2d_kernel(const double* __restrict__ src, int64_t sld, double* dst, int64_t dld,
+                              int64_t rows, int64_t cols) {
+  const int64_t total = rows * cols;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / cols, j = t - (t / cols) * cols;
+    dst[i * dld + j] = src[i * sld + j];
+  }
+}
+
+__global__ void transpose_kernel(const double* __restrict__ src, int64_t sld, double* dst,
+                                 int64_t dld, int64_t rows, int64_t cols) {
+  __shared__ double tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+  // src is cols x rows: src[c * sld + r]
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int64_t c = c0 + j, r = r0 + threadIdx.x;
+    tile[j][threadIdx.x] = (c < cols && r < rows) ? src[c * sld + r] : 0.0;
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int64_t r = r0 + j, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) dst[r * dld + c] = tile[threadIdx.x][j];
+  }
+}
+
+__global__ void combine_kernel(const double* __restrict__ Q, int64_t ldq, int k,
+                               const double* __restrict__ c, const double* y0, double* y,
+                               int64_t n) {
+  __shared__ double cs[256];
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = i0 + threadIdx.x;
+    double v = (y0 && i < n) ? y0[i] : 0.0;
+    for (int c0 = 0; c0 < k; c0 += 256) {
+      const int nc = min(256, k - c0);
+      __syncthreads();
+      for (int j = threadIdx.x; j < nc; j += blockDim.x) cs[j] = c[c0 + j];
+      __syncthreads();
+      if (i < n)
+        for (int j = 0; j < nc; ++j) v = fma(cs[j], Q[(int64_t)(c0 + j) * ldq + i], v);
+    }
+    if (i < n) y[i] = v;
+  }
+}
+
+unsigned ew_grid(int64_t n) {
+  unsigned g = cdiv(n, 256);
+  const unsigned cap = (unsigned)num_sms() * 8;
+  if (g > cap) g = cap;
+  if (g == 0) g = 1;
+  return g;
+}
+
+}  // namespace
+
+int red_blocks(int64_t n) {
+  int64_t g = (n + 2047) / 2048;
+  const int64_t cap = 2 * (int64_t)num_sms();
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+static void red_launch_dims(const RedWS& ws, int64_t n, int nvec, int& G, int64_t& chunk) {
+  G = red_blocks(n);
+  if (G > ws.cap_blocks) G = ws.cap_blocks;
+  chunk = (n + G - 1) / G;
+  chunk = ((chunk + 255) / 256) * 256;
+  if (chunk < 256) chunk = 256;
+  G = (int)((n + chunk - 1) / chunk);
+  if (G < 1) G = 1;
+  TTGB_REQUIRE(nvec <= ws.cap_vec, "reduction workspace too small for the number of vectors");
+}
+
+void nrm2(const RedWS& ws, const double* x, int64_t n, double* out, cudaStream_t s) {
+  int G; int64_t chunk;
+  red_launch_dims(ws, n, 1, G, chunk);
+  nrm2_kernel<<<G, RT, 0, s>>>(x, n, chunk, ws.partial, ws.counter, out, 1);
+  TTGB_CHECK_LAUNCH();
+}
+
+void dot(const RedWS& ws, const double* x, const double* y, int64_t n, double* out, cudaStream_t s) {
+  int G; int64_t chunk;
+  red_launch_dims(ws, n, 1, G, chunk);
+  dot_kernel<<<G, RT, 0, s>>>(x, y, n, chunk, ws.partial, ws.counter, out);
+  TTGB_CHECK_LAUNCH();
+}
+
+void multidot(const RedWS& ws, const double* Q, int64_t ldq, int k, const double* q, int64_t n,
+              double* out, cudaStream_t s) {
+  if (k <= 0) return;
+  int G; int64_t chunk;
+  red_launch_dims(ws, n, k, G, chunk);
+  multidot_kernel<<<G, RT, 0, s>>>(Q, ldq, k, q, n, chunk, ws.partial, ws.counter, out);
+  TTGB_CHECK_LAUNCH();
+}
+
+void gs_update(const RedWS& ws, const double* Q, int64_t ldq, int k, const double* h, double* q,
+               int64_t n, double* out, bool dots, bool sq, cudaStream_t s) {
+  int G; int64_t chunk;
+  red_launch_dims(ws, n, (dots ? k : 0) + (sq ? 1 : 0), G, chunk);
+  gs_update_kernel<<<G, RT, 0, s>>>(Q, ldq, k, h, q, n, chunk, ws.partial, ws.counter, out,
+                                    dots ? 1 : 0, sq ? 1 : 0);
+  TTGB_CHECK_LAUNCH();
+}
+
+void axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  axpby_kernel<<<ew_grid(n), 256, 0, s>>>(a, x, b, y, n);
+  TTGB_CHECK_LAUNCH();
+}
+
+void sub(const double* x, const double* y, double* z, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  sub_kernel<<<ew_grid(n), 256, 0, s>>>(x, y, z, n);
+  TTGB_CHECK_LAUNCH();
+}
+
+void scale_dev(double* x, int64_t n, const double* num, const double* den, cudaStream_t s) {
+  if (n <= 0) return;
+  scale_dev_kernel<<<ew_grid(n), 256, 0, s>>>(x, n, num, den);
+  TTGB_CHECK_LAUNCH();
+}
+
+void scale_copy(const double* x, double a, double* y, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  scale_copy_kernel<<<ew_grid(n), 256, 0, s>>>(x, a, y, n);
+  TTGB_CHECK_LAUNCH();
+}
+
+void fill(double* x, double v, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  fill_kernel<<<ew_grid(n), 256, 0, s>>>(x, v, n);
+  TTGB_CHECK_LAUNCH();
+}
+
+void copy(const double* x, double* y, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  TTGB_CUDA(cudaMemcpyAsync(y, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+}
+
+void copy2d(const double* src, int64_t sld, double* dst, int64_t dld, int64_t rows, int64_t cols,
+            cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return;
+  copy2d_kernel<<<ew_grid(rows * cols), 256, 0, s>>>(src, sld, dst, dld, rows, cols);
+  TTGB_CHECK_LAUNCH();
+}
+
+void transpose(const double* src, int64_t sld, double* dst, int64_t dld, int64_t rows, int64_t cols,
+               cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return;
+  dim3 grid(cdiv(cols, 32), cdiv(rows, 32));
+  TTGB_REQUIRE(grid.y < 65536, "transpose too tall");
+  transpose_kernel<<<grid, dim3(32, 8), 0, s>>>(src, sld, dst, dld, rows, cols);
+  TTGB_CHECK_LAUNCH();
+}
+
+void combine(const double* Q, int64_t ldq, int k, const double* c, const double* y0, double* y,
+             int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  combine_kernel<<<ew_grid(n), 256, 0, s>>>(Q, ldq, k, c, y0, y, n);
+  TTGB_CHECK_LAUNCH();
+}
+
+}  // namespace ttgb

@@ -1,0 +1,51 @@
+// Vector kernels of the AMEn path: deterministic reductions (norms, dots, multi-dots) whose result
+// stays in device memory, and the element-wise updates of the local solves.
+#pragma once
+
+#include "common.cuh"
+
+namespace ttgb {
+
+// Scratch of the two-stage reductions. A reduction launches G blocks that write G partial sums;
+// the last block to finish (atomic ticket) adds them in block order, so results are deterministic.
+struct RedWS {
+  double* partial = nullptr;    // cap_blocks * cap_vec doubles
+  unsigned* counter = nullptr;  // one ticket counter, returned to 0 by the last block
+  int cap_blocks = 0;
+  int cap_vec = 0;
+};
+
+int red_blocks(int64_t n);
+
+// out[0] = ||x||_2 (out[1] = ||x||_2^2 if `both`)
+void nrm2(const RedWS& ws, const double* x, int64_t n, double* out, cudaStream_t s);
+// out[0] = x . y
+void dot(const RedWS& ws, const double* x, const double* y, int64_t n, double* out, cudaStream_t s);
+// out[i] = Q_i . q for i < k; Q_i = Q + i*ldq
+void multidot(const RedWS& ws, const double* Q, int64_t ldq, int k, const double* q, int64_t n,
+              double* out, cudaStream_t s);
+// q <- q - sum_i h[i] Q_i; then, if `dots`, out[i] = Q_i . q (i < k); if `sq`, out[0] = ||q||^2
+void gs_update(const RedWS& ws, const double* Q, int64_t ldq, int k, const double* h, double* q,
+               int64_t n, double* out, bool dots, bool sq, cudaStream_t s);
+
+// y <- a*x + b*y (host scalars)
+void axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream_t s);
+// z <- x - y
+void sub(const double* x, const double* y, double* z, int64_t n, cudaStream_t s);
+// x <- x * (num / den) with device scalars; den <= 0 leaves x unchanged (num may be null: 1)
+void scale_dev(double* x, int64_t n, const double* num, const double* den, cudaStream_t s);
+// y <- x * a (host scalar)
+void scale_copy(const double* x, double a, double* y, int64_t n, cudaStream_t s);
+void fill(double* x, double v, int64_t n, cudaStream_t s);
+void copy(const double* x, double* y, int64_t n, cudaStream_t s);
+// 2-D strided copy: dst[i*dld + j] = src[i*sld + j], i < rows, j < cols
+void copy2d(const double* src, int64_t sld, double* dst, int64_t dld, int64_t rows, int64_t cols,
+            cudaStream_t s);
+// dst (rows x cols, row-major ld) = transpose of src (cols x rows, row-major sld)
+void transpose(const double* src, int64_t sld, double* dst, int64_t dld, int64_t rows, int64_t cols,
+               cudaStream_t s);
+// y = sum_i c[i] * Q_i (+ y0 if y0 != null), c device, Q_i = Q + i*ldq
+void combine(const double* Q, int64_t ldq, int k, const double* c, const double* y0, double* y,
+             int64_t n, cudaStream_t s);
+
+}  // namespace ttgb

@@ -1,0 +1,334 @@
+// extern "C" surface of the library (declared in include/ttgb300.h). Every entry point converts
+// exceptions into status codes and keeps the message in a thread-local buffer.
+#include <cstring>
+#include <string>
+
+#include "../../include/ttgb300.h"
+#include "amen.cuh"
+#include "blas1.cuh"
+#include "contract.cuh"
+#include "gmres.cuh"
+#include "linalg.cuh"
+#include "prec.cuh"
+
+using namespace ttgb;
+
+struct ttgb_solution {
+  AmenResult res;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F>
+int guarded(F&& f) {
+  try {
+    f();
+    return TTGB_OK;
+  } catch (const Error& e) {
+    g_last_error = e.what();
+    return e.status;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return TTGB_ERR_INTERNAL;
+  } catch (...) {
+    g_last_error = "unknown error";
+    return TTGB_ERR_INTERNAL;
+  }
+}
+
+TTView view_of(const ttgb_tt* t, bool matrix) {
+  TTView v;
+  if (!t || t->d <= 0) return v;
+  TTGB_REQUIRE(t->cols && t->ranks && t->cores, "TT descriptor with null arrays");
+  v.d = t->d;
+  v.cols.assign(t->cols, t->cols + t->d);
+  v.ranks.assign(t->ranks, t->ranks + t->d + 1);
+  if (matrix) {
+    TTGB_REQUIRE(t->rows != nullptr, "A must be TT-matrix and b must be vector.");
+    v.rows.assign(t->rows, t->rows + t->d);
+  } else {
+    TTGB_REQUIRE(t->rows == nullptr, "A must be TT-matrix and b must be vector.");
+  }
+  v.cores.assign(t->cores, t->cores + t->d);
+  for (int k = 0; k < t->d; ++k) {
+    TTGB_REQUIRE(v.ranks[k] >= 1 && v.cols[k] >= 1, "Check the ranks and the mode size.");
+    TTGB_REQUIRE(v.cores[k] != nullptr, "null core pointer");
+  }
+  TTGB_REQUIRE(v.ranks[t->d] >= 1, "Check the ranks and the mode size.");
+  return v;
+}
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+struct Scratch {   // per-call workspace of the kernel-level entry points
+  cudaStream_t s;
+  DBuf partial;
+  unsigned* counter = nullptr;
+  RedWS red;
+  LinalgWS lws;
+  char* hbuf = nullptr;
+  explicit Scratch(cudaStream_t st) : s(st) {
+    partial.reset(512 * 128, s);
+    TTGB_CUDA(cudaMallocAsync((void**)&counter, 64, s));
+    TTGB_CUDA(cudaMemsetAsync(counter, 0, 64, s));
+    red.partial = partial.p;
+    red.counter = counter;
+    red.cap_blocks = 512;
+    red.cap_vec = 127;
+    TTGB_CUDA(cudaMallocAsync((void**)&lws.status, 16, s));
+    TTGB_CUDA(cudaMemsetAsync(lws.status, 0, 16, s));
+    TTGB_CUDA(cudaMallocHost((void**)&hbuf, 256));
+    lws.h_status = (int*)hbuf;
+  }
+  ~Scratch() {
+    cudaStreamSynchronize(s);
+    if (counter) cudaFreeAsync(counter, s);
+    if (lws.status) cudaFreeAsync(lws.status, s);
+    if (hbuf) cudaFreeHost(hbuf);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+void ttgb_default_params(ttgb_amen_params* p) {
+  if (!p) return;
+  p->nswp = 22;
+  p->eps = 1e-10;
+  p->rmax = 32768;
+  p->max_full = 500;
+  p->kickrank = 4;
+  p->kick2 = 0;
+  p->local_iterations = 40;
+  p->resets = 2;
+  p->verbose = 0;
+  p->preconditioner = TTGB_PREC_NONE;
+  p->seed = 1;
+  p->profile = 0;
+}
+
+int ttgb_amen_solve(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, const ttgb_tt* z0,
+                    const ttgb_amen_params* params, void* stream, ttgb_solution** out) {
+  return guarded([&] {
+    TTGB_REQUIRE(A && b && params && out, "A, b, params and out must not be NULL");
+    TTView Av = view_of(A, true), bv = view_of(b, false);
+    TTView xv = view_of(x0, false), zv = view_of(z0, false);
+    AmenParams p;
+    p.nswp = params->nswp;
+    p.eps = params->eps;
+    p.rmax = params->rmax;
+    p.max_full = params->max_full;
+    p.kickrank = params->kickrank;
+    p.kick2 = params->kick2;
+    p.local_iterations = params->local_iterations;
+    p.resets = params->resets;
+    p.verbose = params->verbose;
+    p.prec = params->preconditioner;
+    p.seed = params->seed;
+    p.profile = params->profile;
+    auto* sol = new ttgb_solution;
+    try {
+      sol->res = amen_solve(Av, bv, xv, zv, p, as_stream(stream));
+    } catch (...) {
+      delete sol;
+      throw;
+    }
+    *out = sol;
+  });
+}
+
+int ttgb_solution_dims(const ttgb_solution* sol, int32_t* d, int64_t* ranks) {
+  return guarded([&] {
+    TTGB_REQUIRE(sol != nullptr, "null solution");
+    if (d) *d = (int32_t)sol->res.cores.size();
+    if (ranks)
+      for (size_t i = 0; i < sol->res.ranks.size(); ++i) ranks[i] = sol->res.ranks[i];
+  });
+}
+
+int ttgb_solution_stats(const ttgb_solution* sol, ttgb_stats* st) {
+  return guarded([&] {
+    TTGB_REQUIRE(sol && st, "null argument");
+    const AmenStats& a = sol->res.stats;
+    st->sweeps = a.sweeps;
+    st->converged = a.converged;
+    st->max_res = a.max_res;
+    st->local_solves = a.local_solves;
+    st->direct_solves = a.direct_solves;
+    st->gmres_iterations = a.gmres_iterations;
+    st->matvecs = a.matvecs;
+    st->matvec_flops = a.matvec_flops;
+    st->phi_flops = a.phi_flops;
+    st->other_flops = a.other_flops;
+    st->host_syncs = a.host_syncs;
+    st->contract_ms = a.contract_ms;
+    st->contract_launches = a.contract_launches;
+    st->contract_flops = a.contract_flops;
+  });
+}
+
+const double* ttgb_solution_core(const ttgb_solution* sol, int32_t k) {
+  if (!sol || k < 0 || k >= (int32_t)sol->res.cores.size()) return nullptr;
+  return sol->res.cores[k].data();
+}
+
+int ttgb_solution_copy_core(const ttgb_solution* sol, int32_t k, double* dst, int32_t dst_is_host,
+                            void* stream) {
+  return guarded([&] {
+    TTGB_REQUIRE(sol && dst && k >= 0 && k < (int32_t)sol->res.cores.size(), "bad core index");
+    const DTensor& c = sol->res.cores[k];
+    TTGB_CUDA(cudaMemcpyAsync(dst, c.data(), c.numel() * sizeof(double),
+                              dst_is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                              as_stream(stream)));
+    if (dst_is_host) TTGB_CUDA(cudaStreamSynchronize(as_stream(stream)));
+  });
+}
+
+void ttgb_solution_free(ttgb_solution* sol) { delete sol; }
+
+int ttgb_local_product(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, int64_t S,
+                       int64_t RL, int64_t R, const double* phi_l, const double* A,
+                       const double* phi_r, const double* x, double* y, int32_t nrhs,
+                       void* stream) {
+  return guarded([&] {
+    TTGB_REQUIRE(rl > 0 && s > 0 && r > 0 && m > 0 && n > 0 && S > 0 && RL > 0 && R > 0 && nrhs > 0,
+                 "non-positive dimension");
+    TTGB_REQUIRE(phi_l && A && phi_r && x && y, "null pointer");
+    cudaStream_t st = as_stream(stream);
+    LocalOpDims d{rl, s, r, m, n, S, RL, R};
+    DBuf w1(local_product_w1(d), st), w2(local_product_w2(d), st);
+    for (int32_t i = 0; i < nrhs; ++i)
+      local_product(d, phi_l, A, phi_r, x + (int64_t)i * r * n * R, y + (int64_t)i * rl * m * RL,
+                    w1.p, w2.p, st);
+  });
+}
+
+static int phi_A_entry(bool fwd, int64_t l, int64_t L, int64_t s, int64_t S, int64_t r, int64_t R,
+                       int64_t M, int64_t N, const double* phi, const double* left, const double* A,
+                       const double* right, double* out, void* stream) {
+  return guarded([&] {
+    TTGB_REQUIRE(l > 0 && L > 0 && s > 0 && S > 0 && r > 0 && R > 0 && M > 0 && N > 0,
+                 "non-positive dimension");
+    TTGB_REQUIRE(phi && left && A && right && out, "null pointer");
+    cudaStream_t st = as_stream(stream);
+    PhiDims d{l, L, s, S, r, R, M, N};
+    DBuf w(phi_A_workspace(d), st);
+    if (fwd) phi_fwd_A(d, phi, left, A, right, out, w.p, st);
+    else phi_bck_A(d, phi, left, A, right, out, w.p, st);
+  });
+}
+
+int ttgb_phi_fwd_A(int64_t l, int64_t L, int64_t s, int64_t S, int64_t r, int64_t R, int64_t M,
+                   int64_t N, const double* phi, const double* left, const double* A,
+                   const double* right, double* out, void* stream) {
+  return phi_A_entry(true, l, L, s, S, r, R, M, N, phi, left, A, right, out, stream);
+}
+
+int ttgb_phi_bck_A(int64_t l, int64_t L, int64_t s, int64_t S, int64_t r, int64_t R, int64_t M,
+                   int64_t N, const double* phi, const double* left, const double* A,
+                   const double* right, double* out, void* stream) {
+  return phi_A_entry(false, l, L, s, S, r, R, M, N, phi, left, A, right, out, stream);
+}
+
+static int phi_rhs_entry(bool fwd, int64_t b, int64_t B, int64_t r, int64_t R, int64_t n,
+                         const double* phi, const double* core_b, const double* core, double* out,
+                         void* stream) {
+  return guarded([&] {
+    TTGB_REQUIRE(b > 0 && B > 0 && r > 0 && R > 0 && n > 0, "non-positive dimension");
+    TTGB_REQUIRE(phi && core_b && core && out, "null pointer");
+    cudaStream_t st = as_stream(stream);
+    PhiRhsDims d{b, B, r, R, n};
+    DBuf w(phi_rhs_workspace(d), st);
+    if (fwd) phi_fwd_rhs(d, phi, core_b, core, out, w.p, st);
+    else phi_bck_rhs(d, phi, core_b, core, out, w.p, st);
+  });
+}
+
+int ttgb_phi_fwd_rhs(int64_t b, int64_t B, int64_t r, int64_t R, int64_t n, const double* phi,
+                     const double* core_b, const double* core, double* out, void* stream) {
+  return phi_rhs_entry(true, b, B, r, R, n, phi, core_b, core, out, stream);
+}
+
+int ttgb_phi_bck_rhs(int64_t b, int64_t B, int64_t r, int64_t R, int64_t n, const double* phi,
+                     const double* core_b, const double* core, double* out, void* stream) {
+  return phi_rhs_entry(false, b, B, r, R, n, phi, core_b, core, out, stream);
+}
+
+int ttgb_qr(const double* a, int64_t lda, int64_t m, int64_t n, double* q, double* r,
+            void* stream) {
+  return guarded([&] {
+    TTGB_REQUIRE(m > 0 && n > 0 && lda >= m && a && q && r, "bad QR arguments");
+    Scratch sc(as_stream(stream));
+    qr(a, lda, m, n, q, r, sc.lws, sc.red, sc.s);
+    TTGB_CUDA(cudaStreamSynchronize(sc.s));
+  });
+}
+
+int ttgb_svd(const double* a, int64_t lda, int64_t m, int64_t n, double* u, double* s, double* vh,
+             void* stream) {
+  return guarded([&] {
+    TTGB_REQUIRE(m > 0 && n > 0 && lda >= m && a && u && s && vh, "bad SVD arguments");
+    Scratch sc(as_stream(stream));
+    svd(a, lda, m, n, u, s, vh, sc.lws, sc.red, sc.s);
+    TTGB_CUDA(cudaStreamSynchronize(sc.s));
+  });
+}
+
+int ttgb_local_gmres(int64_t r, int64_t s, int64_t n, int64_t S, int64_t R, const double* phi_l,
+                     const double* A, const double* phi_r, const double* rhs, double* x,
+                     int32_t iters, double threshold, int32_t resets, int32_t prec,
+                     int32_t* flag, int32_t* nit, void* stream) {
+  return guarded([&] {
+    TTGB_REQUIRE(r > 0 && s > 0 && n > 0 && S > 0 && R > 0 && iters > 0 && resets > 0,
+                 "bad GMRES arguments");
+    TTGB_REQUIRE(prec >= 0 && prec <= 2, "Invalid preconditioner.");
+    Scratch sc(as_stream(stream));
+    LocalOperator op;
+    op.dims = LocalOpDims{r, s, r, n, n, S, R, R};
+    op.phi_l = phi_l;
+    op.A = A;
+    op.phi_r = phi_r;
+    op.prec = prec;
+    DBuf w1(local_product_w1(op.dims), sc.s), w2(local_product_w2(op.dims), sc.s);
+    op.w1 = w1.p;
+    op.w2 = w2.p;
+    DBuf J, pw, wp, tmp;
+    if (prec) {
+      J.reset(prec_size(prec, op.dims), sc.s);
+      prec_setup(prec, op.dims, phi_l, A, phi_r, J.p, pw, sc.lws.status, sc.s);
+      wp.reset((size_t)op.size(), sc.s);
+      op.J = J.p;
+      op.wp = wp.p;
+    }
+    GmresWS gws;
+    TTGB_CUDA(cudaMallocAsync((void**)&gws.d_flag, 16, sc.s));
+    gws.h_flag = (int*)(sc.hbuf + 64);
+    GmresResult g;
+    try {
+      g = gmres(op, rhs, x, iters, threshold, resets, gws, sc.red, sc.s);
+    } catch (...) {
+      cudaFreeAsync(gws.d_flag, sc.s);
+      throw;
+    }
+    if (prec) {
+      tmp.reset((size_t)op.size(), sc.s);
+      op.apply_prec(x, tmp.p, sc.s);
+      copy(tmp.p, x, op.size(), sc.s);
+    }
+    cudaFreeAsync(gws.d_flag, sc.s);
+    TTGB_CUDA(cudaStreamSynchronize(sc.s));
+    if (flag) *flag = g.flag;
+    if (nit) *nit = g.nit;
+  });
+}
+
+const char* ttgb_last_error(void) { return g_last_error.c_str(); }
+
+int64_t ttgb_launch_count(void) { return launch_count(); }
+
+int32_t ttgb_version(void) { return 100; }
+
+}  // extern "C"

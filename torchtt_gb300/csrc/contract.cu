@@ -1,0 +1,397 @@
+// FP64 contraction engine and the AMEn contraction recipes built on it.
+//
+// The kernel is a shared-memory-tiled FP64 GEMM (BMxBN output tile, BK=16, 256 threads, each
+// thread a (BM/16)x(BN/16) register tile). Every operand index may be a pair of tensor indices with
+// their own strides (struct Ax), so the reference's tensordot permutes (cpp/amen_solve.h:17-98)
+// cost no copies. FP64 FMA throughput is the bound on this path; the tile shape is picked per call
+// so that the grid covers the SMs, and split-K (atomic FP64 adds) is used when even the smallest
+// tile leaves SMs idle.
+#include <climits>
+
+#include "contract.cuh"
+
+namespace ttgb {
+
+namespace {
+
+struct AxD {  // device copy of Ax with a 32-bit inner extent
+  int e0;
+  int64_t s1, s0;
+};
+
+__device__ __forceinline__ int64_t ax_off(const AxD& a, int i) {
+  int i1 = i / a.e0;
+  int i0 = i - i1 * a.e0;
+  return (int64_t)i1 * a.s1 + (int64_t)i0 * a.s0;
+}
+
+struct KParams {
+  int M, N, K, batch, splitk, kchunk;
+  const double* A;
+  AxD am, ak;
+  int64_t a_bs;
+  const double* B;
+  AxD bk, bn;
+  int64_t b_bs;
+  double* C;
+  AxD cm, cn;
+  int64_t c_bs;
+  double alpha, beta;
+};
+
+constexpr int BK = 16;
+constexpr int NT = 256;
+
+template <int BM, int BN>
+__global__ void __launch_bounds__(NT) contract_kernel(KParams p) {
+  constexpr int TM = BM / 16, TN = BN / 16;
+  __shared__ double As[BK][BM + 1];
+  __shared__ double Bs[BK][BN + 1];
+
+  const int tid = threadIdx.x;
+  const int bz = blockIdx.z;
+  const int bidx = bz / p.splitk;
+  const int ks = bz - bidx * p.splitk;
+  const int kbeg = ks * p.kchunk;
+  const int kend = min(p.K, kbeg + p.kchunk);
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+
+  const double* A = p.A + (int64_t)bidx * p.a_bs;
+  const double* B = p.B + (int64_t)bidx * p.b_bs;
+
+  // loader mapping: A tile BM x BK, B tile BK x BN, NT threads
+  constexpr int A_ROWS_PER_PASS = NT / BK;   // threads cover (row, k) with k = tid % BK
+  constexpr int B_COLS_PER_PASS = NT / BK;
+  const int lk = tid % BK;
+  const int lr = tid / BK;   // 0..15
+
+  int64_t a_moff[BM / A_ROWS_PER_PASS];
+  bool a_mok[BM / A_ROWS_PER_PASS];
+#pragma unroll
+  for (int i = 0; i < BM / A_ROWS_PER_PASS; ++i) {
+    int m = m0 + lr + i * A_ROWS_PER_PASS;
+    a_mok[i] = m < p.M;
+    a_moff[i] = a_mok[i] ? ax_off(p.am, m) : 0;
+  }
+  int64_t b_noff[BN / B_COLS_PER_PASS];
+  bool b_nok[BN / B_COLS_PER_PASS];
+#pragma unroll
+  for (int i = 0; i < BN / B_COLS_PER_PASS; ++i) {
+    int n = n0 + lr + i * B_COLS_PER_PASS;
+    b_nok[i] = n < p.N;
+    b_noff[i] = b_nok[i] ? ax_off(p.bn, n) : 0;
+  }
+
+  const int ty = tid / 16, tx = tid % 16;
+  double acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = 0.0;
+
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    const int k = k0 + lk;
+    const bool kok = k < kend;
+    const int64_t a_koff = kok ? ax_off(p.ak, k) : 0;
+    const int64_t b_koff = kok ? ax_off(p.bk, k) : 0;
+#pragma unroll
+    for (int i = 0; i < BM / A_ROWS_PER_PASS; ++i)
+      As[lk][lr + i * A_ROWS_PER_PASS] = (kok && a_mok[i]) ? __ldg(A + a_moff[i] + a_koff) : 0.0;
+#pragma unroll
+    for (int i = 0; i < BN / B_COLS_PER_PASS; ++i)
+      Bs[lk][lr + i * B_COLS_PER_PASS] = (kok && b_nok[i]) ? __ldg(B + b_noff[i] + b_koff) : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+
+  double* C = p.C + (int64_t)bidx * p.c_bs;
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int m = m0 + ty + 16 * i;
+    if (m >= p.M) continue;
+    const int64_t cmo = ax_off(p.cm, m);
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int n = n0 + tx + 16 * j;
+      if (n >= p.N) continue;
+      double* c = C + cmo + ax_off(p.cn, n);
+      const double v = p.alpha * acc[i][j];
+      if (p.splitk > 1) {
+        atomicAdd(c, v);
+      } else {
+        *c = (p.beta == 0.0) ? v : fma(p.beta, *c, v);
+      }
+    }
+  }
+}
+
+// C <- beta * C over the (batched, strided) output index space
+__global__ void scale_output_kernel(double* C, int M, int N, int batch, AxD cm, AxD cn, int64_t c_bs,
+                                    double beta) {
+  const int64_t total = (int64_t)M * N * batch;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int b = (int)(t / ((int64_t)M * N));
+    int rem = (int)(t - (int64_t)b * M * N);
+    int m = rem / N, n = rem - (rem / N) * N;
+    double* c = C + (int64_t)b * c_bs + ax_off(cm, m) + ax_off(cn, n);
+    *c = (beta == 0.0) ? 0.0 : beta * *c;
+  }
+}
+
+AxD to_dev(const Ax& a, int extent) {
+  AxD r;
+  if (a.e0 >= extent || a.e0 >= INT_MAX) {
+    r.e0 = INT_MAX;
+    r.s1 = 0;
+  } else {
+    r.e0 = (int)a.e0;
+    r.s1 = a.s1;
+  }
+  r.s0 = a.s0;
+  return r;
+}
+
+}  // namespace
+
+void contract(const ContractDesc& d, cudaStream_t stream, bool deterministic) {
+  if (d.M <= 0 || d.N <= 0 || d.batch <= 0) return;
+  KParams p;
+  p.M = d.M; p.N = d.N; p.K = d.K; p.batch = d.batch;
+  p.A = d.A; p.am = to_dev(d.am, d.M); p.ak = to_dev(d.ak, d.K); p.a_bs = d.a_bs;
+  p.B = d.B; p.bk = to_dev(d.bk, d.K); p.bn = to_dev(d.bn, d.N); p.b_bs = d.b_bs;
+  p.C = d.C; p.cm = to_dev(d.cm, d.M); p.cn = to_dev(d.cn, d.N); p.c_bs = d.c_bs;
+  p.alpha = d.alpha; p.beta = d.beta;
+  if (d.K <= 0) {  // empty sum: C = beta * C
+    scale_output_kernel<<<cdiv((int64_t)d.M * d.N * d.batch, 256) > 4096 ? 4096 : cdiv((int64_t)d.M * d.N * d.batch, 256), 256, 0, stream>>>(
+        p.C, p.M, p.N, p.batch, p.cm, p.cn, p.c_bs, p.beta);
+    TTGB_CHECK_LAUNCH();
+    return;
+  }
+  const int sms = num_sms();
+  auto tiles = [&](int bm, int bn) { return (int64_t)cdiv(d.M, bm) * cdiv(d.N, bn) * d.batch; };
+  int bm = 64, bn = 64;
+  const int64_t target = 2 * (int64_t)sms;
+  if (tiles(64, 64) < target) {
+    if (d.M >= d.N) { bm = 64; bn = 32; } else { bm = 32; bn = 64; }
+    if (tiles(bm, bn) < target) { bm = 32; bn = 32; }
+  }
+  int splitk = 1;
+  const int64_t t = tiles(bm, bn);
+  if (!deterministic && t < sms && d.K >= 128) {
+    splitk = (int)((target + t - 1) / t);
+    int maxsplit = d.K / 64;
+    if (splitk > maxsplit) splitk = maxsplit;
+    if (splitk < 1) splitk = 1;
+  }
+  int kchunk = d.K;
+  if (splitk > 1) {
+    kchunk = (int)cdiv(cdiv(d.K, splitk), BK) * BK;
+    splitk = (int)cdiv(d.K, kchunk);
+  }
+  p.splitk = splitk;
+  p.kchunk = kchunk;
+  if (splitk > 1) {
+    int64_t total = (int64_t)d.M * d.N * d.batch;
+    unsigned g = cdiv(total, 256);
+    if (g > 8192) g = 8192;
+    scale_output_kernel<<<g, 256, 0, stream>>>(p.C, p.M, p.N, p.batch, p.cm, p.cn, p.c_bs, p.beta);
+    TTGB_CHECK_LAUNCH();
+  }
+  dim3 grid(cdiv(d.N, bn), cdiv(d.M, bm), (unsigned)(d.batch * splitk));
+  TTGB_REQUIRE(grid.y < 65536 && grid.z < 65536, "contraction grid too large");
+  if (bm == 64 && bn == 64) contract_kernel<64, 64><<<grid, NT, 0, stream>>>(p);
+  else if (bm == 64 && bn == 32) contract_kernel<64, 32><<<grid, NT, 0, stream>>>(p);
+  else if (bm == 32 && bn == 64) contract_kernel<32, 64><<<grid, NT, 0, stream>>>(p);
+  else contract_kernel<32, 32><<<grid, NT, 0, stream>>>(p);
+  TTGB_CHECK_LAUNCH();
+}
+
+// --------------------------------------------------------------------------------------------
+// AMEn contraction recipes
+// --------------------------------------------------------------------------------------------
+
+void local_product(const LocalOpDims& d, const double* phi_l, const double* A, const double* phi_r,
+                   const double* x, double* y, double* w1, double* w2, cudaStream_t stream,
+                   double alpha, double beta) {
+  // step 1: W[(l,s),(n,R)] = sum_r Phi_l[(l,s), r] X[r, (n,R)]
+  {
+    ContractDesc c;
+    c.M = (int)(d.rl * d.s); c.N = (int)(d.n * d.R); c.K = (int)d.r;
+    c.A = phi_l; c.am = Ax::one(d.r); c.ak = Ax::one(1);
+    c.B = x; c.bk = Ax::one(d.n * d.R); c.bn = Ax::one(1);
+    c.C = w1; c.cm = Ax::one(d.n * d.R); c.cn = Ax::one(1);
+    contract(c, stream);
+  }
+  // step 2 (batched over l): Y2_l[(m,S), R] = sum_{(s,n)} A[s,m,n,S] W_l[(s,n), R]
+  {
+    ContractDesc c;
+    c.M = (int)(d.m * d.S); c.N = (int)d.R; c.K = (int)(d.s * d.n); c.batch = (int)d.rl;
+    c.A = A; c.am = Ax::two(d.S, d.n * d.S, 1); c.ak = Ax::two(d.n, d.m * d.n * d.S, d.S);
+    c.B = w1; c.bk = Ax::one(d.R); c.bn = Ax::one(1); c.b_bs = d.s * d.n * d.R;
+    c.C = w2; c.cm = Ax::one(d.R); c.cn = Ax::one(1); c.c_bs = d.m * d.S * d.R;
+    contract(c, stream);
+  }
+  // step 3: y[(l,m), L] = alpha * sum_{(S,R)} Y2[(l,m),(S,R)] Phi_r[L,(S,R)] + beta * y
+  {
+    ContractDesc c;
+    c.M = (int)(d.rl * d.m); c.N = (int)d.RL; c.K = (int)(d.S * d.R);
+    c.A = w2; c.am = Ax::one(d.S * d.R); c.ak = Ax::one(1);
+    c.B = phi_r; c.bk = Ax::one(1); c.bn = Ax::one(d.S * d.R);
+    c.C = y; c.cm = Ax::one(d.RL); c.cn = Ax::one(1);
+    c.alpha = alpha; c.beta = beta;
+    contract(c, stream);
+  }
+}
+
+size_t phi_A_workspace(const PhiDims& d) {
+  size_t fwd = size_t(d.s * d.r * d.M * d.L + d.r * d.L * d.N * d.S);
+  size_t bck = size_t(d.l * d.M * d.S * d.R + d.l * d.s * d.N * d.R);
+  return fwd > bck ? fwd : bck;
+}
+
+void phi_fwd_A(const PhiDims& d, const double* phi, const double* left, const double* A,
+               const double* right, double* out, double* work, cudaStream_t stream) {
+  double* T1 = work;                              // [s, r, M, L]
+  double* T2 = work + d.s * d.r * d.M * d.L;      // [r, L, N, S]
+  {  // T1[(s,r),(M,L)] = sum_l Phi[l,(s,r)] left[l,(M,L)]
+    ContractDesc c;
+    c.M = (int)(d.s * d.r); c.N = (int)(d.M * d.L); c.K = (int)d.l;
+    c.A = phi; c.am = Ax::one(1); c.ak = Ax::one(d.s * d.r);
+    c.B = left; c.bk = Ax::one(d.M * d.L); c.bn = Ax::one(1);
+    c.C = T1; c.cm = Ax::one(d.M * d.L); c.cn = Ax::one(1);
+    contract(c, stream);
+  }
+  {  // T2[(r,L),(N,S)] = sum_{(s,M)} T1[s,r,M,L] A[s,M,N,S]
+    ContractDesc c;
+    c.M = (int)(d.r * d.L); c.N = (int)(d.N * d.S); c.K = (int)(d.s * d.M);
+    c.A = T1; c.am = Ax::two(d.L, d.M * d.L, 1); c.ak = Ax::two(d.M, d.r * d.M * d.L, d.L);
+    c.B = A; c.bk = Ax::two(d.M, d.M * d.N * d.S, d.N * d.S); c.bn = Ax::one(1);
+    c.C = T2; c.cm = Ax::one(d.N * d.S); c.cn = Ax::one(1);
+    contract(c, stream);
+  }
+  {  // out[L,S,R] = sum_{(r,N)} T2[r,L,N,S] right[r,N,R]   (batched over S)
+    ContractDesc c;
+    c.M = (int)d.L; c.N = (int)d.R; c.K = (int)(d.r * d.N); c.batch = (int)d.S;
+    c.A = T2; c.am = Ax::one(d.N * d.S); c.ak = Ax::two(d.N, d.L * d.N * d.S, d.S); c.a_bs = 1;
+    c.B = right; c.bk = Ax::one(d.R); c.bn = Ax::one(1);
+    c.C = out; c.cm = Ax::one(d.S * d.R); c.cn = Ax::one(1); c.c_bs = d.R;
+    contract(c, stream);
+  }
+}
+
+void phi_bck_A(const PhiDims& d, const double* phi, const double* left, const double* A,
+               const double* right, double* out, double* work, cudaStream_t stream) {
+  double* T1 = work;                              // [l, M, S, R]
+  double* T2 = work + d.l * d.M * d.S * d.R;      // [l, s, N, R]
+  {  // T1[(l,M),(S,R)] = sum_L left[(l,M), L] Phi[L,(S,R)]
+    ContractDesc c;
+    c.M = (int)(d.l * d.M); c.N = (int)(d.S * d.R); c.K = (int)d.L;
+    c.A = left; c.am = Ax::one(d.L); c.ak = Ax::one(1);
+    c.B = phi; c.bk = Ax::one(d.S * d.R); c.bn = Ax::one(1);
+    c.C = T1; c.cm = Ax::one(d.S * d.R); c.cn = Ax::one(1);
+    contract(c, stream);
+  }
+  {  // T2[l,s,N,R] = sum_{(M,S)} T1[l,M,S,R] A[s,M,N,S]; rows (l,R), cols (s,N)
+    ContractDesc c;
+    c.M = (int)(d.l * d.R); c.N = (int)(d.s * d.N); c.K = (int)(d.M * d.S);
+    c.A = T1; c.am = Ax::two(d.R, d.M * d.S * d.R, 1); c.ak = Ax::two(d.S, d.S * d.R, d.R);
+    c.B = A; c.bk = Ax::two(d.S, d.N * d.S, 1); c.bn = Ax::two(d.N, d.M * d.N * d.S, d.S);
+    c.C = T2; c.cm = Ax::two(d.R, d.s * d.N * d.R, 1); c.cn = Ax::two(d.N, d.N * d.R, d.R);
+    contract(c, stream);
+  }
+  {  // out[(l,s), r] = sum_{(N,R)} T2[(l,s),(N,R)] right[r,(N,R)]
+    ContractDesc c;
+    c.M = (int)(d.l * d.s); c.N = (int)d.r; c.K = (int)(d.N * d.R);
+    c.A = T2; c.am = Ax::one(d.N * d.R); c.ak = Ax::one(1);
+    c.B = right; c.bk = Ax::one(1); c.bn = Ax::one(d.N * d.R);
+    c.C = out; c.cm = Ax::one(d.r); c.cn = Ax::one(1);
+    contract(c, stream);
+  }
+}
+
+size_t phi_rhs_workspace(const PhiRhsDims& d) {
+  size_t f = size_t(d.n * d.B * d.r), b = size_t(d.b * d.n * d.R);
+  return f > b ? f : b;
+}
+
+void phi_fwd_rhs(const PhiRhsDims& d, const double* phi, const double* core_b, const double* core,
+                 double* out, double* work, cudaStream_t stream) {
+  {  // T[(n,B), r] = sum_b core_b[b,(n,B)] Phi[b, r]
+    ContractDesc c;
+    c.M = (int)(d.n * d.B); c.N = (int)d.r; c.K = (int)d.b;
+    c.A = core_b; c.am = Ax::one(1); c.ak = Ax::one(d.n * d.B);
+    c.B = phi; c.bk = Ax::one(d.r); c.bn = Ax::one(1);
+    c.C = work; c.cm = Ax::one(d.r); c.cn = Ax::one(1);
+    contract(c, stream);
+  }
+  {  // out[B, R] = sum_{(r,n)} T[n,B,r] core[r,n,R]
+    ContractDesc c;
+    c.M = (int)d.B; c.N = (int)d.R; c.K = (int)(d.r * d.n);
+    c.A = work; c.am = Ax::one(d.r); c.ak = Ax::two(d.n, 1, d.B * d.r);
+    c.B = core; c.bk = Ax::one(d.R); c.bn = Ax::one(1);
+    c.C = out; c.cm = Ax::one(d.R); c.cn = Ax::one(1);
+    contract(c, stream);
+  }
+}
+
+void phi_bck_rhs(const PhiRhsDims& d, const double* phi, const double* core_b, const double* core,
+                 double* out, double* work, cudaStream_t stream) {
+  {  // T[(b,n), R] = sum_B core_b[(b,n), B] Phi[B, R]
+    ContractDesc c;
+    c.M = (int)(d.b * d.n); c.N = (int)d.R; c.K = (int)d.B;
+    c.A = core_b; c.am = Ax::one(d.B); c.ak = Ax::one(1);
+    c.B = phi; c.bk = Ax::one(d.R); c.bn = Ax::one(1);
+    c.C = work; c.cm = Ax::one(d.R); c.cn = Ax::one(1);
+    contract(c, stream);
+  }
+  {  // out[b, r] = sum_{(n,R)} T[b,(n,R)] core[r,(n,R)]
+    ContractDesc c;
+    c.M = (int)d.b; c.N = (int)d.r; c.K = (int)(d.n * d.R);
+    c.A = work; c.am = Ax::one(d.n * d.R); c.ak = Ax::one(1);
+    c.B = core; c.bk = Ax::one(1); c.bn = Ax::one(d.n * d.R);
+    c.C = out; c.cm = Ax::one(d.r); c.cn = Ax::one(1);
+    contract(c, stream);
+  }
+}
+
+size_t local_rhs_workspace(int64_t b, int64_t n, int64_t B, int64_t r, int64_t R) {
+  (void)B; (void)r;
+  return size_t(b * n * R);
+}
+
+void local_rhs(int64_t b, int64_t n, int64_t B, int64_t r, int64_t R, const double* phi_l,
+               const double* core_b, const double* phi_r, double alpha, double* out, double* work,
+               cudaStream_t stream) {
+  {  // T[(b,n), R] = sum_B core_b[(b,n),B] Phi_r[B,R]
+    ContractDesc c;
+    c.M = (int)(b * n); c.N = (int)R; c.K = (int)B;
+    c.A = core_b; c.am = Ax::one(B); c.ak = Ax::one(1);
+    c.B = phi_r; c.bk = Ax::one(R); c.bn = Ax::one(1);
+    c.C = work; c.cm = Ax::one(R); c.cn = Ax::one(1);
+    contract(c, stream);
+  }
+  {  // out[r, (n,R)] = alpha * sum_b Phi_l[b, r] T[b, (n,R)]
+    ContractDesc c;
+    c.M = (int)r; c.N = (int)(n * R); c.K = (int)b;
+    c.A = phi_l; c.am = Ax::one(1); c.ak = Ax::one(r);
+    c.B = work; c.bk = Ax::one(n * R); c.bn = Ax::one(1);
+    c.C = out; c.cm = Ax::one(n * R); c.cn = Ax::one(1);
+    c.alpha = alpha;
+    contract(c, stream);
+  }
+}
+
+}  // namespace ttgb

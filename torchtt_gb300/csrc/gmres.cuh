@@ -1,0 +1,58 @@
+// Local AMEn operator and the restarted GMRES that solves with it
+// (reference: AMENsolveMV, cpp/matvecs.h:130-212; gmres / gmres_single, cpp/gmres.h:34-161).
+#pragma once
+
+#include "blas1.cuh"
+#include "contract.cuh"
+#include "profiler.cuh"
+
+namespace ttgb {
+
+// algorithmic flops of one local product: 2 rl n R (s r) + 2 rl m S R (s n) + 2 rl m RL (S R)
+inline double local_product_flops(const LocalOpDims& d) {
+  return 2.0 * d.rl * d.n * d.R * (double)d.s * d.r + 2.0 * d.rl * d.m * d.S * (double)d.R * d.s * d.n +
+         2.0 * d.rl * d.m * (double)d.RL * d.S * d.R;
+}
+
+enum Prec : int { kNoPrec = 0, kCPrec = 1, kRPrec = 2 };   // cpp/define.h:10-12
+
+// y = B x with B = Phi_left x A_k x Phi_right (the projected operator), optionally composed with
+// the block-Jacobi preconditioner P: y = B (P x).
+struct LocalOperator {
+  LocalOpDims dims{};
+  const double* phi_l = nullptr;
+  const double* A = nullptr;
+  const double* phi_r = nullptr;
+  int prec = kNoPrec;
+  const double* J = nullptr;    // preconditioner blocks (see prec.cu)
+  double* w1 = nullptr;         // local_product workspaces
+  double* w2 = nullptr;
+  double* wp = nullptr;         // preconditioned input (N_loc)
+  Profiler* prof = nullptr;     // optional launch timing
+  int64_t* count = nullptr;     // optional: incremented per application
+  int64_t size() const { return dims.r * dims.n * dims.R; }
+  void apply(const double* x, double* y, bool use_prec, cudaStream_t s) const;
+  void apply_prec(const double* x, double* y, cudaStream_t s) const;
+};
+
+struct GmresWS {
+  DBuf Q;        // (iters + 1) x n Krylov basis
+  DBuf small;    // H, cs, sn, beta, h1, h2, scalars
+  int* h_flag = nullptr;   // pinned: converged flag, iteration count
+  int* d_flag = nullptr;
+};
+
+struct GmresResult {
+  int flag = 0;   // 1 when the threshold was reached (gmres.h:125-129)
+  int nit = 0;    // total iterations over all restarts
+};
+
+// Restarted GMRES from x0 = 0: solves op(x) = rhs with relative threshold `threshold` on the
+// residual reduction |beta_{k+1}| / ||rhs||, at most `iters` iterations per cycle and `resets`
+// cycles. The orthogonalisation is classical Gram-Schmidt applied twice (CGS2), which is as
+// stable as the reference's modified Gram-Schmidt and needs 3 passes over the basis instead of
+// 2(k+1) dependent ones; Givens rotations and the convergence test run on the device.
+GmresResult gmres(const LocalOperator& op, const double* rhs, double* sol, int iters,
+                  double threshold, int resets, GmresWS& ws, const RedWS& red, cudaStream_t s);
+
+}  // namespace ttgb

@@ -1,0 +1,544 @@
+// FP64 dense linear algebra: shifted CholeskyQR3 with a Householder fallback, one-sided Jacobi
+// thin SVD, LU solve with partial pivoting.
+//
+// GB300 note: FP64 runs at ~1.9 FMA/clock/SM (measured), so every O(m n^2) step is expressed as a
+// GEMM on the contraction engine (spread over all SMs); only O(n^3) steps on the small n x n
+// factors (Cholesky, triangular inverse, Jacobi) run inside one thread block.
+#include <cmath>
+
+#include "contract.cuh"
+#include "linalg.cuh"
+
+namespace ttgb {
+
+namespace {
+
+constexpr double kEps = 2.220446049250313e-16;
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ double block_sum_d(double v, double* sh) {
+  v = warp_sum_d(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += sh[i];
+  __syncthreads();
+  return r;   // valid in all threads
+}
+
+__device__ double block_max_d(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r = fmax(r, sh[i]);
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Cholesky of the symmetric n x n matrix G (row-major, in place -> upper R with G = R^T R).
+// shift_rows > 0 adds the sCholQR3 shift 11 (m n + n (n+1)) eps ||A||_F^2 with m = shift_rows
+// (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa, SIAM J. Sci. Comput. 2020).
+// check_identity: flag status=2 when max |G - I| > 0.1 (the third pass of CholeskyQR3 sees the
+// Gram matrix of an already orthonormalised Q).
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) chol_kernel(double* G, int n, int64_t shift_rows,
+                                                   int check_identity, int* status) {
+  __shared__ double sh[32];
+  __shared__ int bad;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  if (check_identity) {
+    double mx = 0.0;
+    for (int64_t t = tid; t < (int64_t)n * n; t += nt) {
+      const int i = (int)(t / n), k = (int)(t % n);
+      const double v = G[t] - (i == k ? 1.0 : 0.0);
+      mx = fmax(mx, isfinite(v) ? fabs(v) : 1e300);
+    }
+    mx = block_max_d(mx, sh);
+    if (tid == 0 && !(mx <= 0.1)) *status = 2;
+  }
+  if (shift_rows > 0) {
+    double tr = 0.0;
+    for (int i = tid; i < n; i += nt) tr += G[(int64_t)i * n + i];
+    tr = block_sum_d(tr, sh);
+    const double sft = 11.0 * ((double)shift_rows * n + (double)n * (n + 1)) * kEps * tr;
+    for (int i = tid; i < n; i += nt) G[(int64_t)i * n + i] += sft;
+  }
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    const double d = G[(int64_t)j * n + j];
+    if (!(d > 0.0) || !isfinite(d)) {
+      if (tid == 0) { bad = 1; *status = 1; }
+    }
+    __syncthreads();
+    if (bad) break;
+    const double rd = sqrt(d);
+    for (int k = j + 1 + tid; k < n; k += nt) G[(int64_t)j * n + k] /= rd;
+    __syncthreads();
+    if (tid == 0) G[(int64_t)j * n + j] = rd;
+    const int w = n - j - 1;
+    for (int64_t t = tid; t < (int64_t)w * w; t += nt) {
+      const int i = j + 1 + (int)(t / w), k = j + 1 + (int)(t % w);
+      if (k < i) continue;
+      G[(int64_t)i * n + k] = fma(-G[(int64_t)j * n + i], G[(int64_t)j * n + k], G[(int64_t)i * n + k]);
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  for (int64_t t = tid; t < (int64_t)n * n; t += nt) {
+    const int i = (int)(t / n), k = (int)(t % n);
+    if (k < i) G[t] = 0.0;
+  }
+}
+
+// Ri = R^{-1} for the upper-triangular row-major R (one thread per column of Ri).
+__global__ void trinv_kernel(const double* __restrict__ R, double* Ri, int n) {
+  for (int j = threadIdx.x + blockIdx.x * blockDim.x; j < n; j += blockDim.x * gridDim.x) {
+    for (int i = n - 1; i >= 0; --i) {
+      double v = (i == j) ? 1.0 : 0.0;
+      if (i <= j) {
+        for (int k = i + 1; k <= j; ++k) v = fma(-R[(int64_t)i * n + k], Ri[(int64_t)k * n + j], v);
+        v /= R[(int64_t)i * n + i];
+      }
+      Ri[(int64_t)i * n + j] = (i <= j) ? v : 0.0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Single-block Householder QR (LAPACK dgeqrf/dorgqr scheme): W (m x n col-major, ld m) is
+// overwritten; outputs Q (m x k, ld m) and R (k x n, ld k), k = min(m, n).
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) householder_kernel(double* W, int m, int n, double* Q,
+                                                          double* R, double* tau) {
+  __shared__ double sh[32];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const int k = min(m, n);
+  for (int j = 0; j < k; ++j) {
+    double* col = W + (int64_t)j * m;
+    double xs = 0.0;
+    for (int i = j + 1 + tid; i < m; i += nt) xs = fma(col[i], col[i], xs);
+    xs = block_sum_d(xs, sh);
+    const double alpha = col[j];
+    const double nrm = sqrt(alpha * alpha + xs);
+    double tj = 0.0, beta = alpha, scale = 0.0;
+    if (xs > 0.0) {
+      beta = -copysign(nrm, alpha);
+      tj = (beta - alpha) / beta;
+      scale = 1.0 / (alpha - beta);
+    }
+    for (int i = j + 1 + tid; i < m; i += nt) col[i] *= scale;
+    __syncthreads();
+    if (tid == 0) { col[j] = beta; tau[j] = tj; }
+    __syncthreads();
+    if (tj != 0.0) {
+      for (int c = j + 1 + warp; c < n; c += nw) {
+        double* cc = W + (int64_t)c * m;
+        const double c0 = cc[j];   // read by every lane before lane 0 updates it
+        double w = 0.0;
+        for (int i = j + 1 + lane; i < m; i += 32) w = fma(col[i], cc[i], w);
+        w = warp_sum_d(w) + c0;
+        const double tw = tj * w;
+        if (lane == 0) cc[j] -= tw;
+        for (int i = j + 1 + lane; i < m; i += 32) cc[i] = fma(-tw, col[i], cc[i]);
+      }
+    }
+    __syncthreads();
+  }
+  // R = upper part
+  for (int64_t t = tid; t < (int64_t)k * n; t += nt) {
+    const int i = (int)(t % k), c = (int)(t / k);
+    R[t] = (i <= c) ? W[(int64_t)c * m + i] : 0.0;
+  }
+  // Q = H_0 ... H_{k-1} [I; 0]
+  for (int64_t t = tid; t < (int64_t)m * k; t += nt) {
+    const int i = (int)(t % m), c = (int)(t / m);
+    Q[t] = (i == c) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  for (int j = k - 1; j >= 0; --j) {
+    const double tj = tau[j];
+    if (tj == 0.0) continue;
+    const double* col = W + (int64_t)j * m;
+    for (int c = j + warp; c < k; c += nw) {
+      double* qc = Q + (int64_t)c * m;
+      const double q0 = qc[j];
+      double w = 0.0;
+      for (int i = j + 1 + lane; i < m; i += 32) w = fma(col[i], qc[i], w);
+      w = warp_sum_d(w) + q0;
+      const double tw = tj * w;
+      if (lane == 0) qc[j] -= tw;
+      for (int i = j + 1 + lane; i < m; i += 32) qc[i] = fma(-tw, col[i], qc[i]);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// One-sided (Hestenes) Jacobi SVD of the n x n column-major matrix W in one thread block, with
+// the round-robin parallel ordering; rotation formulas of Demmel & Veselic (SIAM J. Matrix Anal.
+// Appl. 13, 1992). On exit U (n x n) holds W_j / sigma_j, V the accumulated rotations, both with
+// columns sorted by descending sigma, S the sorted singular values.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ int rr_index(int p, int r, int nn) {
+  return p == 0 ? 0 : ((p - 1 + r) % (nn - 1)) + 1;
+}
+
+__global__ void __launch_bounds__(512) jacobi_svd_kernel(double* Wg, double* Vg, int n, double* U,
+                                                         double* S, int use_smem, int max_sweeps,
+                                                         int* status) {
+  extern __shared__ double smem[];
+  __shared__ int nrot;
+  double* W = use_smem ? smem : Wg;
+  double* V = use_smem ? smem + (int64_t)n * n : Vg;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  if (use_smem) {
+    for (int64_t t = tid; t < (int64_t)n * n; t += nt) W[t] = Wg[t];
+  }
+  for (int64_t t = tid; t < (int64_t)n * n; t += nt) V[t] = ((t % n) == (t / n)) ? 1.0 : 0.0;
+  __syncthreads();
+  const int nn = n + (n & 1);
+  const double tol = fmax((double)n, 1.0) * kEps;
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (tid == 0) nrot = 0;
+    __syncthreads();
+    for (int r = 0; r < nn - 1; ++r) {
+      for (int pi = warp; pi < nn / 2; pi += nw) {
+        int p = rr_index(pi, r, nn), q = rr_index(nn - 1 - pi, r, nn);
+        if (p > q) { const int t = p; p = q; q = t; }
+        if (q >= n) continue;
+        double* wp = W + (int64_t)p * n;
+        double* wq = W + (int64_t)q * n;
+        double a = 0.0, b = 0.0, g = 0.0;
+        for (int i = lane; i < n; i += 32) {
+          const double x = wp[i], y = wq[i];
+          a = fma(x, x, a); b = fma(y, y, b); g = fma(x, y, g);
+        }
+        a = warp_sum_d(a); b = warp_sum_d(b); g = warp_sum_d(g);
+        if (a == 0.0 || b == 0.0) continue;
+        if (!(fabs(g) > tol * sqrt(a) * sqrt(b))) continue;
+        const double zeta = (b - a) / (2.0 * g);
+        double t;
+        if (fabs(zeta) > 1e150) t = 0.5 / zeta;
+        else t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+        for (int i = lane; i < n; i += 32) {
+          const double x = wp[i], y = wq[i];
+          wp[i] = c * x - s * y;
+          wq[i] = s * x + c * y;
+        }
+        double* vp = V + (int64_t)p * n;
+        double* vq = V + (int64_t)q * n;
+        for (int i = lane; i < n; i += 32) {
+          const double x = vp[i], y = vq[i];
+          vp[i] = c * x - s * y;
+          vq[i] = s * x + c * y;
+        }
+        if (lane == 0) atomicAdd(&nrot, 1);
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+    if (nrot == 0) break;
+    __syncthreads();
+  }
+  if (tid == 0 && sweep >= max_sweeps) *status = 3;
+  // singular values, ranks by descending value (ties by index)
+  double* sig = S;  // temporary: write unsorted to S via registers below
+  for (int j = warp; j < n; j += nw) {
+    const double* wj = W + (int64_t)j * n;
+    double a = 0.0;
+    for (int i = lane; i < n; i += 32) a = fma(wj[i], wj[i], a);
+    a = warp_sum_d(a);
+    if (lane == 0) U[(int64_t)j] = sqrt(a);   // stash sigma_j in U's first column temporarily
+  }
+  __syncthreads();
+  // rank computation, then write sorted S (U column 0 is rewritten afterwards)
+  __shared__ int rank_sh[1024];
+  for (int j = tid; j < n; j += nt) {
+    const double sj = U[j];
+    int rk = 0;
+    for (int i = 0; i < n; ++i) {
+      const double si = U[i];
+      rk += (si > sj) || (si == sj && i < j);
+    }
+    if (j < 1024) rank_sh[j] = rk;
+  }
+  __syncthreads();
+  for (int j = tid; j < n; j += nt) sig[rank_sh[j]] = U[j];
+  __syncthreads();
+  // U[:, rank_j] = W_j / sigma_j ; V columns permuted into Wg (scratch) then copied back
+  for (int j = warp; j < n; j += nw) {
+    const int rk = rank_sh[j];
+    const double sj = sig[rk];
+    const double inv = sj > 0.0 ? 1.0 / sj : 0.0;
+    const double* wj = W + (int64_t)j * n;
+    for (int i = lane; i < n; i += 32) Vg[(int64_t)n * n + (int64_t)rk * n + i] = wj[i] * inv;
+  }
+  __syncthreads();
+  for (int64_t t = tid; t < (int64_t)n * n; t += nt) U[t] = Vg[(int64_t)n * n + t];
+  __syncthreads();
+  for (int j = warp; j < n; j += nw) {
+    const int rk = rank_sh[j];
+    const double* vj = V + (int64_t)j * n;
+    for (int i = lane; i < n; i += 32) Vg[(int64_t)n * n + (int64_t)rk * n + i] = vj[i];
+  }
+  __syncthreads();
+  for (int64_t t = tid; t < (int64_t)n * n; t += nt) Vg[t] = Vg[(int64_t)n * n + t];
+}
+
+// ---------------------------------------------------------------------------------------------
+// LU with partial pivoting on an n x n row-major copy, solving for one right-hand side.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) lu_solve_kernel(double* LU, double* x, int n, int* status) {
+  __shared__ double shv[32];
+  __shared__ int shi[32];
+  __shared__ int piv;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int j = 0; j < n; ++j) {
+    // pivot search
+    double best = -1.0;
+    int bi = j;
+    for (int i = j + tid; i < n; i += nt) {
+      const double v = fabs(LU[(int64_t)i * n + j]);
+      if (v > best) { best = v; bi = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    if (lane == 0) { shv[warp] = best; shi[warp] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      double b = -1.0; int ib = j;
+      for (int w = 0; w < (nt >> 5); ++w)
+        if (shv[w] > b || (shv[w] == b && shi[w] < ib)) { b = shv[w]; ib = shi[w]; }
+      piv = ib;
+      if (!(b > 0.0)) *status = 1;
+    }
+    __syncthreads();
+    const int p = piv;
+    if (p != j) {
+      for (int c = tid; c < n; c += nt) {
+        const double t = LU[(int64_t)j * n + c];
+        LU[(int64_t)j * n + c] = LU[(int64_t)p * n + c];
+        LU[(int64_t)p * n + c] = t;
+      }
+      if (tid == 0) { const double t = x[j]; x[j] = x[p]; x[p] = t; }
+    }
+    __syncthreads();
+    const double dj = LU[(int64_t)j * n + j];
+    const int w = n - j - 1;
+    // multipliers
+    for (int i = j + 1 + tid; i < n; i += nt) LU[(int64_t)i * n + j] /= dj;
+    __syncthreads();
+    for (int i = j + 1 + tid; i < n; i += nt) x[i] = fma(-LU[(int64_t)i * n + j], x[j], x[i]);
+    for (int64_t t = tid; t < (int64_t)w * w; t += nt) {
+      const int i = j + 1 + (int)(t / w), c = j + 1 + (int)(t % w);
+      LU[(int64_t)i * n + c] = fma(-LU[(int64_t)i * n + j], LU[(int64_t)j * n + c], LU[(int64_t)i * n + c]);
+    }
+    __syncthreads();
+  }
+  // back substitution
+  __shared__ double shs[32];
+  for (int i = n - 1; i >= 0; --i) {
+    double s = 0.0;
+    for (int c = i + 1 + tid; c < n; c += nt) s = fma(LU[(int64_t)i * n + c], x[c], s);
+    s = warp_sum_d(s);
+    if (lane == 0) shs[warp] = s;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w2 = 0; w2 < (nt >> 5); ++w2) t += shs[w2];
+      x[i] = (x[i] - t) / LU[(int64_t)i * n + i];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void gemv_rm_kernel(const double* __restrict__ B, int64_t n, const double* __restrict__ x,
+                               double* y) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (row >= n) return;
+  double s = 0.0;
+  for (int64_t c = lane; c < n; c += 32) s = fma(B[row * n + c], x[c], s);
+  s = warp_sum_d(s);
+  if (lane == 0) y[row] = s;
+}
+
+__global__ void copy_cm_kernel(const double* __restrict__ A, int64_t lda, double* W, int64_t m,
+                               int64_t n) {
+  const int64_t total = m * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % m, j = t / m;
+    W[t] = A[j * lda + i];
+  }
+}
+
+void read_status(LinalgWS& ws, cudaStream_t s, int* out) {
+  TTGB_CUDA(cudaMemcpyAsync(ws.h_status, ws.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  TTGB_CUDA(cudaStreamSynchronize(s));
+  *out = *ws.h_status;
+}
+
+void householder(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, double* R,
+                 LinalgWS& ws, cudaStream_t s) {
+  const int64_t k = m < n ? m : n;
+  ws.d.ensure(m * n + k + 16, s);
+  double* W = ws.d.p;
+  double* tau = W + m * n;
+  unsigned g = cdiv(m * n, 256);
+  if (g > 4096) g = 4096;
+  if (g == 0) g = 1;
+  copy_cm_kernel<<<g, 256, 0, s>>>(A, lda, W, m, n);
+  TTGB_CHECK_LAUNCH();
+  householder_kernel<<<1, 512, 0, s>>>(W, (int)m, (int)n, Q, R, tau);
+  TTGB_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+void gemm_cm(const double* A, int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
+             int64_t m, int64_t n, int64_t k, double alpha, double beta, cudaStream_t s,
+             bool transA, bool transB) {
+  ContractDesc c;
+  c.M = (int)m; c.N = (int)n; c.K = (int)k;
+  c.A = A;
+  if (!transA) { c.am = Ax::one(1); c.ak = Ax::one(lda); }
+  else { c.am = Ax::one(lda); c.ak = Ax::one(1); }
+  c.B = B;
+  if (!transB) { c.bk = Ax::one(1); c.bn = Ax::one(ldb); }
+  else { c.bk = Ax::one(ldb); c.bn = Ax::one(1); }
+  c.C = C; c.cm = Ax::one(1); c.cn = Ax::one(ldc);
+  c.alpha = alpha; c.beta = beta;
+  contract(c, s);
+}
+
+QRResult qr(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, double* R,
+            LinalgWS& ws, const RedWS& red, cudaStream_t s) {
+  (void)red;
+  QRResult res;
+  res.k = m < n ? m : n;
+  if (m <= 0 || n <= 0) return res;
+  // small, wide: single-block Householder (robust, cheap at these sizes)
+  const bool small = (double)m * n * n < 4.0e5;
+  if (m < n || small || n > 1024) {
+    householder(A, lda, m, n, Q, R, ws, s);
+    return res;
+  }
+  // shifted CholeskyQR3
+  ws.a.ensure(4 * n * n + 16, s);
+  double* G = ws.a.p;           // n x n Gram / Cholesky factor (row-major R)
+  double* Ri = G + n * n;       // inverse of the current factor
+  double* Rt = Ri + n * n;      // accumulated R (row-major)
+  double* Tm = Rt + n * n;      // temporary
+  ws.b.ensure(m * n + 16, s);
+  double* Qt = ws.b.p;
+  TTGB_CUDA(cudaMemsetAsync(ws.status, 0, sizeof(int), s));
+  const double* Ain = A;
+  int64_t ldin = lda;
+  double* outs[3] = {Q, Qt, Q};
+  for (int pass = 0; pass < 3; ++pass) {
+    gemm_cm(Ain, ldin, Ain, ldin, G, n, n, n, m, 1.0, 0.0, s, true, false);
+    chol_kernel<<<1, 512, 0, s>>>(G, (int)n, pass == 0 ? m : 0, pass == 2 ? 1 : 0, ws.status);
+    TTGB_CHECK_LAUNCH();
+    trinv_kernel<<<cdiv(n, 128), 128, 0, s>>>(G, Ri, (int)n);
+    TTGB_CHECK_LAUNCH();
+    // Q_next = Ain * R^{-1}   (Ri row-major == (Ri)^T column-major)
+    gemm_cm(Ain, ldin, Ri, n, outs[pass], m, m, n, n, 1.0, 0.0, s, false, true);
+    if (pass == 0) {
+      copy(G, Rt, n * n, s);
+    } else {  // Rt <- R_pass * Rt  (row-major products via column-major transposes)
+      gemm_cm(Rt, n, G, n, Tm, n, n, n, n, 1.0, 0.0, s, false, false);
+      copy(Tm, Rt, n * n, s);
+    }
+    Ain = outs[pass];
+    ldin = m;
+  }
+  int st = 0;
+  read_status(ws, s, &st);
+  if (st != 0) {
+    householder(A, lda, m, n, Q, R, ws, s);
+    return res;
+  }
+  // R (n x n col-major, ld n) from the row-major Rt
+  transpose(Rt, n, R, n, n, n, s);
+  return res;
+}
+
+void svd(const double* A, int64_t lda, int64_t m, int64_t n, double* U, double* S, double* Vh,
+         LinalgWS& ws, const RedWS& red, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return;
+  if (m < n) {
+    // A^T = U' S V'^T  ->  A = V' S U'^T
+    DBuf At((size_t)(n * m), s);
+    transpose(A, lda, At.p, n, m, n, s);      // At (n x m col-major): At[j + i*n] = A[i + j*lda]
+    // transpose() writes dst[r*dld + c] = src[c*sld + r] with rows=m? use explicit kernel via gemm
+    DBuf Ut((size_t)(n * m), s), Vt((size_t)(m * m), s);
+    svd(At.p, n, n, m, Ut.p, S, Vt.p, ws, red, s);
+    // U = V' = Vt^T (m x m); Vh = U'^T (m x n)
+    transpose(Vt.p, m, U, m, m, m, s);
+    transpose(Ut.p, n, Vh, m, n, m, s);
+    return;
+  }
+  // m >= n: A = Q R, R = Ur S V^T
+  DBuf Qb((size_t)(m * n), s), Rb((size_t)(n * n), s);
+  qr(A, lda, m, n, Qb.p, Rb.p, ws, red, s);
+  ws.c.ensure(3 * n * n + 16, s);
+  double* W = ws.c.p;        // n x n working copy of R
+  double* Vw = W + n * n;    // 2 n x n: V and scratch
+  copy(Rb.p, W, n * n, s);
+  DBuf Ur((size_t)(n * n), s);
+  const size_t smem = (size_t)2 * n * n * sizeof(double);
+  const int use_smem = smem <= 200 * 1024 ? 1 : 0;
+  if (use_smem) {
+    TTGB_CUDA(cudaFuncSetAttribute(jacobi_svd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  }
+  TTGB_REQUIRE(n <= 1024, "SVD: too many columns");
+  jacobi_svd_kernel<<<1, 512, use_smem ? smem : 0, s>>>(W, Vw, (int)n, Ur.p, S, use_smem, 60,
+                                                         ws.status);
+  TTGB_CHECK_LAUNCH();
+  // U = Q Ur
+  gemm_cm(Qb.p, m, Ur.p, n, U, m, m, n, n, 1.0, 0.0, s);
+  // Vh (n x n col-major) = V^T
+  transpose(Vw, n, Vh, n, n, n, s);
+}
+
+void lu_solve(const double* B, int64_t n, const double* rhs, double* x, LinalgWS& ws,
+              cudaStream_t s) {
+  ws.e.ensure(n * n + 16, s);
+  copy(B, ws.e.p, n * n, s);
+  copy(rhs, x, n, s);
+  lu_solve_kernel<<<1, 1024, 0, s>>>(ws.e.p, x, (int)n, ws.status);
+  TTGB_CHECK_LAUNCH();
+}
+
+void gemv(const double* B, int64_t n, const double* x, double* y, cudaStream_t s) {
+  if (n <= 0) return;
+  gemv_rm_kernel<<<cdiv(n * 32, 256), 256, 0, s>>>(B, n, x, y);
+  TTGB_CHECK_LAUNCH();
+}
+
+}  // namespace ttgb

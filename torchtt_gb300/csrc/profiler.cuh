@@ -1,0 +1,58 @@
+// Optional CUDA-event timing of the contraction launches of a solve (AmenParams::profile).
+// Pairs of events bracket each local product / interface update on the solve's stream; the pool is
+// drained (one synchronisation) when full and at the end of the solve.
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace ttgb {
+
+struct Profiler {
+  cudaStream_t s = nullptr;
+  std::vector<cudaEvent_t> pool;
+  std::vector<double> pending_flops;
+  std::vector<int> pending_launches;
+  size_t used = 0;
+  double ms = 0.0;
+  int64_t launches = 0;
+  double flops = 0.0;
+
+  explicit Profiler(cudaStream_t st, size_t pairs = 2048) : s(st) {
+    pool.resize(2 * pairs);
+    for (auto& e : pool) TTGB_CUDA(cudaEventCreate(&e));
+  }
+  ~Profiler() {
+    for (auto& e : pool) cudaEventDestroy(e);
+  }
+  Profiler(const Profiler&) = delete;
+  Profiler& operator=(const Profiler&) = delete;
+
+  void begin() {
+    if (used + 2 > pool.size()) flush();
+    TTGB_CUDA(cudaEventRecord(pool[used], s));
+  }
+  void end(double f, int nlaunch) {
+    TTGB_CUDA(cudaEventRecord(pool[used + 1], s));
+    pending_flops.push_back(f);
+    pending_launches.push_back(nlaunch);
+    used += 2;
+  }
+  void flush() {
+    if (used == 0) return;
+    TTGB_CUDA(cudaEventSynchronize(pool[used - 1]));
+    for (size_t i = 0; i < used; i += 2) {
+      float t = 0.f;
+      TTGB_CUDA(cudaEventElapsedTime(&t, pool[i], pool[i + 1]));
+      ms += t;
+    }
+    for (double f : pending_flops) flops += f;
+    for (int l : pending_launches) launches += l;
+    pending_flops.clear();
+    pending_launches.clear();
+    used = 0;
+  }
+};
+
+}  // namespace ttgb

@@ -1,0 +1,144 @@
+"""The tensor-train type at the solver boundary.
+
+``TT`` mirrors the parts of the reference's ``torchtt.TT`` (``torchtt/_tt_base.py:18-229``) that
+the AMEn path uses: construction from a list of cores with the same rank checks and errors, the
+``cores``/``N``/``M``/``R``/``is_ttm`` properties, device moves, and the algebra the reference's
+tests apply to a solution (``A @ x``, ``x - b``, ``.norm()``; ``tests/test_solvers.py:19``).
+The solver also accepts the reference's own ``torchtt.TT`` objects (anything with ``cores`` and
+``is_ttm``) and returns an object of the same class as ``b``.
+"""
+import torch
+
+from .errors import IncompatibleTypes, InvalidArguments, RankMismatch, ShapeMismatch
+
+
+class TT:
+    def __init__(self, cores):
+        if not isinstance(cores, (list, tuple)) or len(cores) == 0:
+            raise InvalidArguments("TT expects a non-empty list of cores.")
+        cores = list(cores)
+        R = [cores[0].shape[0]]
+        N, M = [], []
+        for i, c in enumerate(cores):   # torchtt/_tt_base.py:123-161
+            s = c.shape
+            if s[0] != R[-1]:
+                raise RankMismatch("Ranks of the given cores do not match: for core number %d previous "
+                                   "rank is %d and and current rank is %d." % (i, R[-1], s[0]))
+            if len(s) == 3:
+                R.append(s[2]); N.append(s[1])
+            elif len(s) == 4:
+                R.append(s[3]); M.append(s[1]); N.append(s[2])
+            else:
+                raise InvalidArguments("Invalid input: TT-cores have to be either 4d or 3d.")
+        if R[0] != 1 or R[-1] != 1 or (len(M) != 0 and len(M) != len(N)):
+            raise InvalidArguments("Check the ranks and the mode size.")
+        self.cores = cores
+        self._R = [int(r) for r in R]
+        self._N = [int(n) for n in N]
+        self._M = [int(m) for m in M]
+        self._is_ttm = len(M) == len(N)
+
+    # -- properties ------------------------------------------------------------------------
+    @property
+    def is_ttm(self):
+        return self._is_ttm
+
+    @property
+    def N(self):
+        return list(self._N)
+
+    @property
+    def M(self):
+        if not self._is_ttm:
+            raise IncompatibleTypes("The field is_ttm is defined only for TT matrices.")
+        return list(self._M)
+
+    @property
+    def R(self):
+        return list(self._R)
+
+    @property
+    def shape(self):
+        return [(m, n) for m, n in zip(self._M, self._N)] if self._is_ttm else list(self._N)
+
+    def __repr__(self):
+        kind = "TT-matrix" if self._is_ttm else "TT"
+        return "%s with sizes %s, ranks %s, device %s" % (kind, self.shape, self._R, self.cores[0].device)
+
+    # -- device / dtype ----------------------------------------------------------------------
+    def to(self, device=None, dtype=None):
+        return TT([c.to(device=device, dtype=dtype) for c in self.cores])
+
+    def cuda(self, device=None):
+        return TT([c.cuda(device) for c in self.cores])
+
+    def cpu(self):
+        return TT([c.cpu() for c in self.cores])
+
+    def clone(self):
+        return TT([c.clone() for c in self.cores])
+
+    # -- algebra used to check solutions ------------------------------------------------------
+    def __matmul__(self, other):
+        """TT-matrix @ TT-vector core by core (torchtt/_tt_base.py:807-817): ranks multiply."""
+        if not (self._is_ttm and not other.is_ttm):
+            raise IncompatibleTypes("Only TT-matrix @ TT-vector is supported here.")
+        if self._N != list(other.N):
+            raise ShapeMismatch("Shapes are incompatible.")
+        out = []
+        for a, c in zip(self.cores, other.cores):
+            t = torch.einsum("smnS,rnR->srmSR", a, c)
+            out.append(t.reshape(a.shape[0] * c.shape[0], a.shape[1], a.shape[3] * c.shape[2]))
+        return TT(out)
+
+    def _combine(self, other, beta):
+        if self._is_ttm or other.is_ttm:
+            raise IncompatibleTypes("Only TT-vectors can be added here.")
+        if self._N != list(other.N):
+            raise ShapeMismatch("Shapes are incompatible.")
+        d = len(self.cores)
+        a_c, b_c = self.cores, list(other.cores)
+        if d == 1:
+            return TT([a_c[0] + beta * b_c[0]])
+        out = []
+        for k in range(d):
+            a, b = a_c[k], b_c[k]
+            if k == 0:
+                out.append(torch.cat([a, beta * b], dim=2))
+            elif k == d - 1:
+                out.append(torch.cat([a, b], dim=0))
+            else:
+                c = torch.zeros((a.shape[0] + b.shape[0], a.shape[1], a.shape[2] + b.shape[2]),
+                                dtype=a.dtype, device=a.device)
+                c[:a.shape[0], :, :a.shape[2]] = a
+                c[a.shape[0]:, :, a.shape[2]:] = b
+                out.append(c)
+        return TT(out)
+
+    def __add__(self, other):
+        return self._combine(other, 1.0)
+
+    def __sub__(self, other):
+        return self._combine(other, -1.0)
+
+    def __mul__(self, alpha):
+        return TT([self.cores[0] * alpha] + self.cores[1:])
+
+    __rmul__ = __mul__
+
+    def norm(self):
+        """Frobenius norm by a left-to-right QR sweep (torchtt/_tt_base.py:1021-1051)."""
+        cur = None
+        for c in self.cores:
+            if c.dim() == 4:
+                c = c.reshape(c.shape[0], c.shape[1] * c.shape[2], c.shape[3])
+            if cur is not None:
+                c = torch.tensordot(cur, c, dims=([1], [0]))
+            _, cur = torch.linalg.qr(c.reshape(-1, c.shape[-1]))
+        return torch.linalg.norm(cur)
+
+    def full(self):
+        t = self.cores[0]
+        for c in self.cores[1:]:
+            t = torch.tensordot(t, c, dims=([t.dim() - 1], [0]))
+        return t.reshape(t.shape[1:-1])
