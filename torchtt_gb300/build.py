@@ -47,7 +47,7 @@ def build(verbose=False, jobs=None):
     """Compile and link; returns the path of the shared library."""
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
-    hdr = _newest_header()
+    hdr = max(_newest_header(), os.path.getmtime(os.path.abspath(__file__)))
     srcs = sources()
     objs = []
     todo = []
@@ -59,7 +59,7 @@ def build(verbose=False, jobs=None):
 
     def compile_one(so):
         s, o = so
-        cmd = [nvcc] + ARCH + FLAGS + ["-c", s, "-o", o]
+        cmd = [nvcc] + ARCH + FLAGS + ["-cudart", "shared", "-c", s, "-o", o]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (s, r.stdout, r.stderr))
@@ -74,7 +74,8 @@ def build(verbose=False, jobs=None):
     newest_obj = max(os.path.getmtime(o) for o in objs)
     if todo or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest_obj:
         tmp = LIB + ".tmp"
-        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs
+        # the CUDA runtime is linked dynamically so that the process holds one runtime (torch's)
+        cmd = [nvcc] + ARCH + ["-shared", "-cudart", "shared", "-o", tmp] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

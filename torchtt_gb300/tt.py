@@ -127,9 +127,12 @@ class TT:
     __rmul__ = __mul__
 
     def norm(self):
-        """Frobenius norm by a left-to-right QR sweep (torchtt/_tt_base.py:1021-1051)."""
+        """Frobenius norm by a left-to-right QR sweep (torchtt/_tt_base.py:1021-1051).
+
+        A checking utility, not part of the solver: the small QR factorisations run on the CPU."""
         cur = None
         for c in self.cores:
+            c = c.detach().cpu()
             if c.dim() == 4:
                 c = c.reshape(c.shape[0], c.shape[1] * c.shape[2], c.shape[3])
             if cur is not None:
