@@ -115,6 +115,21 @@ int ttgb_local_product(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, i
                        int64_t RL, int64_t R, const double* phi_l, const double* A,
                        const double* phi_r, const double* x, double* y, int32_t nrhs, void* stream);
 
+/* The same product as ttgb_local_product for callers that must not allocate device memory while
+ * they run (a serving loop that reserved its HBM up front and admits work by footprint, code inside
+ * another framework's memory manager, latency-bound code that cannot take cudaMalloc's implicit
+ * synchronisation). No counterpart in the reference. It calls no cudaMalloc/cudaFree: its two
+ * contraction intermediates live in one static device array of 4 Mi doubles (32 MiB) that every
+ * GPU loading the library holds until process exit, so rl*s*n*R + rl*m*S*R must not exceed
+ * 4194304 (larger requests return TTGB_ERR_INVALID with a message in ttgb_last_error()). The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture. All calls share the array: calls that
+ * overlap on the GPU race and must be ordered by the caller. */
+int ttgb_local_product_noalloc(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, int64_t S,
+                               int64_t RL, int64_t R, const double* phi_l, const double* A,
+                               const double* phi_r, const double* x, double* y, int32_t nrhs,
+                               void* stream);
+
 /* Interface updates (replace compute_phi_fwd_A / compute_phi_bck_A / compute_phi_fwd_rhs /
  * compute_phi_bck_rhs, cpp/amen_solve.h:58-68, 38-47, 93-98, 78-83).
  *   fwd_A: phi[l,s,r], left[l,M,L], A[s,M,N,S], right[r,N,R] -> out[L,S,R]

@@ -56,6 +56,7 @@ _SIGS = {
     "ttgb_solution_copy_core": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp]),
     "ttgb_solution_free": (None, [c_vp]),
     "ttgb_local_product": (c_i32, [c_i64] * 8 + [c_vp] * 5 + [c_i32, c_vp]),
+    "ttgb_local_product_noalloc": (c_i32, [c_i64] * 8 + [c_vp] * 5 + [c_i32, c_vp]),
     "ttgb_phi_fwd_A": (c_i32, [c_i64] * 8 + [c_vp] * 5 + [c_vp]),
     "ttgb_phi_bck_A": (c_i32, [c_i64] * 8 + [c_vp] * 5 + [c_vp]),
     "ttgb_phi_fwd_rhs": (c_i32, [c_i64] * 5 + [c_vp] * 4 + [c_vp]),

@@ -92,6 +92,10 @@ struct Scratch {   // per-call workspace of the kernel-level entry points
 
 }  // namespace
 
+namespace ttgb {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace ttgb
+
 extern "C" {
 
 void ttgb_default_params(ttgb_amen_params* p) {
