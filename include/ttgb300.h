@@ -63,7 +63,15 @@ typedef struct ttgb_amen_params {
   int32_t preconditioner;
   uint64_t seed;
   int32_t profile;              /* 1: time the contraction launches with CUDA events (stats) */
+  int32_t precision;            /* TTGB_PRECISION_FP64 (default) or TTGB_PRECISION_MIXED */
 } ttgb_amen_params;
+
+/* Precision modes. FP64: the reference's arithmetic. MIXED: the local GMRES applies the projected
+ * operator with a low-precision contraction engine inside FP64 iterative refinement (true
+ * residuals, orthogonalisation, QR/SVD and the interfaces stay FP64); the analogue of the
+ * reference's Python-only use_single_precision (torchtt/solvers.py:469-496). */
+#define TTGB_PRECISION_FP64 0
+#define TTGB_PRECISION_MIXED 1
 
 /* Per-solve statistics. */
 typedef struct ttgb_stats {
@@ -81,6 +89,12 @@ typedef struct ttgb_stats {
   double contract_ms;           /* profile only: device time of the contraction kernels */
   int64_t contract_launches;    /* profile only: number of contraction kernel launches */
   double contract_flops;        /* profile only: algorithmic flops of those launches */
+  int64_t lowp_matvecs;         /* mixed: low-precision local products */
+  double lowp_flops;            /* mixed: their algorithmic flops */
+  int64_t refinements;          /* mixed: FP64 refinement steps */
+  double phase_ms[12];          /* profile only: stream time per sweep step - backward z, backward
+                                   QR, backward interfaces, forward setup, local solve, SVD, rank
+                                   search, forward z, enrichment, forward interfaces, other */
 } ttgb_stats;
 
 typedef struct ttgb_solution ttgb_solution;   /* opaque, library-owned result */

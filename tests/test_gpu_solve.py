@@ -74,3 +74,39 @@ def test_edge_cases(cuda):
     x0 = TT([c.to(cuda) for c in W.random_tt([10] * 4, [1, 6, 6, 6, 1], 10)])
     x = amen_solve(A, b, x0=x0, eps=1e-9)
     assert float((A @ x - b).norm() / b.norm()) < 1e-7
+
+
+@pytest.mark.parametrize("fixture", G.solve_fixtures())
+def test_mixed_solve_matches_reference(cuda, fixture):
+    """The mixed-precision path meets the same parity bar against the reference's FP64 solution."""
+    from torchtt_gb300 import TT, amen_solve
+    z = G.load(fixture)
+    A, b = G.cores(z, "A"), G.cores(z, "b")
+    x0, z0 = G.cores(z, "x0"), G.cores(z, "z0")
+    p = G.params(z)
+    prec = {0: None, 1: "c", 2: "r"}[int(z["prec"])]
+    x, st = amen_solve(TT(to_dev(A, cuda)), TT(to_dev(b, cuda)), nswp=p["nswp"],
+                       x0=TT(to_dev(x0, cuda)) if x0 is not None else None, eps=p["eps"],
+                       rmax=p["rmax"], max_full=p["max_full"], kickrank=p["kickrank"],
+                       kick2=p["kick2"], local_iterations=p["local_iterations"], resets=p["resets"],
+                       preconditioner=prec, z0=to_dev(z0, cuda), return_stats=True,
+                       precision="mixed")
+    xs = [c.cpu().numpy() for c in x.cores]
+    cond = _parity.dense_cond(A) if int(np.prod([a.shape[1] for a in A])) <= 2000 else None
+    _parity.check(A, b, xs, G.cores(z, "x_cpp"), p["eps"], p["kickrank"], cond=cond,
+                  label=fixture + " mixed")
+
+
+def test_mixed_equals_fp64_on_laplace(cuda):
+    """Mixed and plain FP64 solves of the d=8 n=16 Laplacian agree to the solve tolerance."""
+    from torchtt_gb300 import TT, amen_solve, workloads as W
+    wl = W.laplace_d8_n16(3)
+    A, b = TT([c.to(cuda) for c in wl["A"]]), TT([c.to(cuda) for c in wl["b"]])
+    x64, s64 = amen_solve(A, b, eps=1e-10, nswp=20, kickrank=4, seed=5, return_stats=True)
+    xmx, smx = amen_solve(A, b, eps=1e-10, nswp=20, kickrank=4, seed=5, return_stats=True,
+                          precision="mixed")
+    r64 = float((A @ x64 - b).norm() / b.norm())
+    rmx = float((A @ xmx - b).norm() / b.norm())
+    assert rmx <= max(1e-9, 2 * r64), (rmx, r64)
+    assert float((xmx - x64).norm() / x64.norm()) <= 1e-9
+    assert smx["lowp_matvecs"] > 0 and smx["refinements"] > 0

@@ -115,7 +115,10 @@ class AmenRun {
     gws_.h_flag = (int*)(hbuf_ + 16);
     hscal_ = (double*)(hbuf_ + 64);
     dscal_.reset(kScal, s_);
-    if (p.profile) prof_.reset(new Profiler(s_));
+    if (p.profile) {
+      prof_.reset(new Profiler(s_));
+      phases_.reset(new PhaseTimer(s_));
+    }
   }
   ~AmenRun() {
     cudaStreamSynchronize(s_);
@@ -153,9 +156,21 @@ class AmenRun {
   AmenStats st_;
   std::unique_ptr<Profiler> prof_;
   int64_t op_count_ = 0;   // applications of the current local operator
+  int64_t lowp_count_ = 0; // low-precision applications of the current local operator
+  bool mixed_ = false;
+  std::vector<FBuf> A32_;  // FP32 copies of the A cores (mixed path)
+  FBuf phil32_, phir32_, xf_, yf_, w1f_, w2f_;
+  DBuf resvec_;
   uint64_t rng_offset_ = 0;
 
   double* slot(int i) { return dscal_.p + i; }
+
+  enum Phase { kPhBwdZ = 0, kPhBwdQR, kPhBwdPhi, kPhFwdSetup, kPhFwdSolve, kPhFwdSvd, kPhFwdRank,
+               kPhFwdZ, kPhFwdEnrich, kPhFwdPhi, kPhOther };
+  std::unique_ptr<PhaseTimer> phases_;
+  void phase(int p) {
+    if (phases_) phases_->mark(p);
+  }
 
   void read_scalars(int n) {
     TTGB_CUDA(cudaMemcpyAsync(hscal_, dscal_.p, n * sizeof(double), cudaMemcpyDeviceToHost, s_));
@@ -250,6 +265,10 @@ class AmenRun {
   void backward_step(int k, int swp, bool last);
   void forward_step(int k, int swp, bool last, double& max_res);
   void z_update_forward(int k, const double* trunc);
+  void setup_lowp(LocalOperator& op, int k);
+  int rank_search_tail(const double* U, const double* SVh, int64_t a, int64_t bdim, int64_t kf,
+                       const double* resvec, double norm_rhs, double thr, const LocalOperator& op,
+                       int64_t nl, double* tail_buf);
   int rank_search(const double* U, const double* SVh, int64_t a, int64_t bdim, int64_t kf,
                   const double* rhs, double norm_rhs, double thr, const LocalOperator* op,
                   const double* B, int64_t nl, double* cand_buf);
@@ -257,6 +276,15 @@ class AmenRun {
 
 void AmenRun::init(const TTView& x0, const TTView& z0) {
   const int d = d_;
+  mixed_ = p_.precision == 1;
+  if (mixed_) {
+    A32_.resize(d);
+    for (int i = 0; i < d; ++i) {
+      const int64_t ne = rA_[i] * N_[i] * N_[i] * rA_[i + 1];
+      A32_[i].reset((size_t)ne, s_);
+      cast(Acore(i), A32_[i].p, ne, s_);
+    }
+  }
   x_.resize(d);
   rx_.assign(d + 1, 1);
   if (x0.d == 0) {   // amen_solve.h:161-163
@@ -317,6 +345,7 @@ void AmenRun::rl_orthogonal_z() {
 
 void AmenRun::backward_step(int k, int swp, bool last) {
   const int64_t n = N_[k];
+  phase(kPhBwdZ);
   if (!last) {   // z update, amen_solve.h:223-245
     DBuf czm;      // column-major (n * rz_{k+1}) x kc matrix of new z directions
     int64_t X = n * rz_[k + 1], kc = 0;
@@ -350,6 +379,7 @@ void AmenRun::backward_step(int k, int swp, bool last) {
   const double nrmsc_before = nrmsc_;
   const double nA0 = normA_[k - 1], nx0 = normx_[k - 1], nb0 = normb_[k - 1];
 
+  phase(kPhBwdQR);
   // QR of x_k^T, absorb R into x_{k-1} (amen_solve.h:252-267)
   const int64_t r = rx_[k], m = n * rx_[k + 1];
   const int64_t kk = r < m ? r : m;
@@ -365,6 +395,7 @@ void AmenRun::backward_step(int k, int swp, bool last) {
   x_[k] = std::move(Q);
   x_[k - 1] = std::move(prev);
 
+  phase(kPhBwdPhi);
   // interfaces (amen_solve.h:270-282)
   phi_A(false, Phis_[k + 1], x_[k].data(), rx_[k], rx_[k + 1], x_[k].data(), rx_[k], rx_[k + 1], k,
         Phis_[k]);
@@ -439,6 +470,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
   const double damp = 2.0;
   const double real_tol = (p_.eps / std::sqrt((double)d_)) / damp;   // amen_solve.h:309
 
+  phase(kPhFwdSetup);
   DBuf rhs((size_t)nl, s_), sol((size_t)nl, s_), tmp((size_t)nl, s_);
   lrhs(Phis_b_[k].data(), rk, k, Phis_b_[k + 1].data(), rk1, nrmsc_, rhs.p);   // :303-304
   const double* prev = x_[k].data();
@@ -448,6 +480,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
   LocalOperator op;
   DBuf Bmat;
   double res_old = 0.0, res_new = 0.0, norm_rhs = 0.0;
+  phase(kPhFwdSolve);
   if (use_full) {   // amen_solve.h:319-330
     st_.direct_solves++;
     Bmat.reset((size_t)(nl * nl), s_);
@@ -487,28 +520,62 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
       op.J = prec_J_.p;
       op.wp = wp_.p;
     }
+    if (mixed_) setup_lowp(op, k);
+    resvec_.ensure((size_t)nl, s_);
     DBuf drhs((size_t)nl, s_);
-    op.apply(prev, drhs.p, false, s_);
+    op.apply_fp64(prev, drhs.p, s_);
     axpby(1.0, rhs.p, -1.0, drhs.p, nl, s_);   // drhs = rhs - B x_prev
     nrm2(red_, rhs.p, nl, slot(kNormRhs), s_);
     nrm2(red_, drhs.p, nl, slot(kNormDrhs), s_);
     read_scalars(2);
     norm_rhs = hscal_[kNormRhs];
     const double nd = hscal_[kNormDrhs];
-    const double eps_local = real_tol * norm_rhs / nd;
-    GmresResult gr = gmres(op, drhs.p, sol.p, p_.local_iterations, eps_local, p_.resets, gws_, red_, s_);
-    st_.gmres_iterations += gr.nit;
-    if (p_.prec != kNoPrec) {
-      op.apply_prec(sol.p, tmp.p, s_);
-      copy(tmp.p, sol.p, nl, s_);
-    }
-    axpby(1.0, prev, 1.0, sol.p, nl, s_);   // solution_now += previous_solution
-    op.apply(sol.p, tmp.p, false, s_);
-    sub(tmp.p, rhs.p, tmp.p, nl, s_);
-    nrm2(red_, tmp.p, nl, slot(kResNew), s_);
-    read_scalars(3);
     res_old = nd / norm_rhs;   // == ||B x_prev - rhs|| / ||rhs|| (amen_solve.h:357)
-    res_new = hscal_[kResNew] / norm_rhs;
+    if (!mixed_) {
+      const double eps_local = real_tol * norm_rhs / nd;
+      GmresResult gr = gmres(op, drhs.p, sol.p, p_.local_iterations, eps_local, p_.resets, gws_, red_, s_);
+      st_.gmres_iterations += gr.nit;
+      if (p_.prec != kNoPrec) {
+        op.apply_prec(sol.p, tmp.p, s_);
+        copy(tmp.p, sol.p, nl, s_);
+      }
+      axpby(1.0, prev, 1.0, sol.p, nl, s_);   // solution_now += previous_solution
+      op.apply_fp64(sol.p, tmp.p, s_);
+      sub(tmp.p, rhs.p, tmp.p, nl, s_);
+      nrm2(red_, tmp.p, nl, slot(kResNew), s_);
+      read_scalars(3);
+      res_new = hscal_[kResNew] / norm_rhs;
+    } else {
+      // FP64 iterative refinement around a GMRES whose operator runs in low precision: every
+      // outer step solves B d = rhs - B x to the low-precision floor, adds d, and recomputes the
+      // true residual in FP64 (amen_solve.h:340-358 with the local solve split into steps).
+      copy(prev, sol.p, nl, s_);
+      const double target = real_tol * norm_rhs;
+      double cur = nd;
+      DBuf dx((size_t)nl, s_);
+      for (int it = 0; it < p_.max_refine && cur > target; ++it) {
+        double thr = target / cur;
+        if (thr < p_.lowp_floor) thr = p_.lowp_floor;
+        GmresResult gr = gmres(op, drhs.p, dx.p, p_.local_iterations, thr, p_.resets, gws_, red_, s_);
+        st_.gmres_iterations += gr.nit;
+        st_.refinements++;
+        if (p_.prec != kNoPrec) {
+          op.apply_prec(dx.p, tmp.p, s_);
+          copy(tmp.p, dx.p, nl, s_);
+        }
+        axpby(1.0, dx.p, 1.0, sol.p, nl, s_);
+        op.apply_fp64(sol.p, tmp.p, s_);
+        sub(rhs.p, tmp.p, drhs.p, nl, s_);      // drhs = rhs - B x
+        nrm2(red_, drhs.p, nl, slot(kResNew), s_);
+        read_scalars(3);
+        const double nw = hscal_[kResNew];
+        const bool stalled = nw > 0.5 * cur;
+        cur = nw;
+        if (stalled) break;
+      }
+      res_new = cur / norm_rhs;
+      scale_copy(drhs.p, -1.0, resvec_.p, nl, s_);   // B x - rhs for the rank search
+    }
   }
   if (p_.verbose && res_old / res_new < damp && res_new > real_tol)
     std::printf("WARNING: residual increase. res_old %g, res_new %g, %g\n", res_old, res_new, real_tol);
@@ -516,6 +583,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
 
   const int64_t a = rk * n, bdim = rk1;
   if (k < d_ - 1) {
+    phase(kPhFwdSvd);
     // SVD of the (r_k n) x r_{k+1} unfolding (amen_solve.h:383)
     const int64_t kf = a < bdim ? a : bdim;
     DBuf Mc((size_t)(a * bdim), s_), U((size_t)(a * kf), s_), S((size_t)kf, s_), SVh((size_t)(kf * bdim), s_);
@@ -523,16 +591,14 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
     svd(Mc.p, a, a, bdim, U.p, S.p, SVh.p, lws_, red_, s_);
     scale_rows_cm_kernel<<<grid_of(kf * bdim), 256, 0, s_>>>(SVh.p, kf, kf, bdim, S.p);
     TTGB_CHECK_LAUNCH();
+    phase(kPhFwdRank);
     const double thr = res_new > real_tol * damp ? res_new : real_tol * damp;
-    int64_t r = rank_search(U.p, SVh.p, a, bdim, kf, rhs.p, norm_rhs, thr, use_full ? nullptr : &op,
-                            Bmat.p, nl, tmp.p);
+    int64_t r = (mixed_ && !use_full)
+                    ? rank_search_tail(U.p, SVh.p, a, bdim, kf, resvec_.p, norm_rhs, thr, op, nl, tmp.p)
+                    : rank_search(U.p, SVh.p, a, bdim, kf, rhs.p, norm_rhs, thr,
+                                  use_full ? nullptr : &op, Bmat.p, nl, tmp.p);
     r += 1;   // amen_solve.h:401-403
     r = (r < kf && r < p_.rmax) ? r : (kf < p_.rmax ? kf : p_.rmax);
-    if (!use_full) {
-      st_.matvecs += op_count_;
-      st_.matvec_flops += op_count_ * lp_flops(op.dims);
-      op_count_ = 0;
-    }
 
     // truncated solution u v^T (row-major a x b) into tmp
     {
@@ -543,11 +609,13 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
       cd.C = tmp.p; cd.cm = Ax::one(bdim); cd.cn = Ax::one(1);
       contract(cd, s_);
     }
+    phase(kPhFwdZ);
     if (!last) z_update_forward(k, tmp.p);
 
     int64_t k2 = r;
     DBuf newx;            // x_k as row-major (rk, n, k2)
     DBuf vprime;          // V' (bdim x k2) column-major
+    phase(kPhFwdEnrich);
     if (!last) {   // enrichment, amen_solve.h:444-460
       // width of the residual block = rows of Phiz[k+1] (the z update above may already have
       // changed rz[k+1]; the reference takes it from the tensor shape, amen_solve.h:452)
@@ -590,6 +658,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
     x_[k + 1] = std::move(xn1);
     rx_[k + 1] = k2;
 
+    phase(kPhFwdPhi);
     // next interfaces (amen_solve.h:482-503)
     phi_A(true, Phis_[k], x_[k].data(), rk, k2, x_[k].data(), rk, k2, k, Phis_[k + 1]);
     phi_b(true, Phis_b_[k], x_[k].data(), rk, k2, k, Phis_b_[k + 1]);
@@ -622,6 +691,76 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
     copy(sol.p, xk.data(), nl, s_);
     x_[k] = std::move(xk);
   }
+  if (!use_full) {
+    st_.matvecs += op_count_;
+    st_.matvec_flops += op_count_ * lp_flops(op.dims);
+    st_.lowp_matvecs += lowp_count_;
+    st_.lowp_flops += lowp_count_ * lp_flops(op.dims);
+    op_count_ = 0;
+    lowp_count_ = 0;
+  }
+}
+
+// FP32 copies of the local operator for the low-precision engine (mixed path)
+void AmenRun::setup_lowp(LocalOperator& op, int k) {
+  const LocalOpDims& d = op.dims;
+  phil32_.ensure((size_t)(d.rl * d.s * d.r), s_);
+  phir32_.ensure((size_t)(d.RL * d.S * d.R), s_);
+  cast(Phis_[k].data(), phil32_.p, d.rl * d.s * d.r, s_);
+  cast(Phis_[k + 1].data(), phir32_.p, d.RL * d.S * d.R, s_);
+  const size_t nl = (size_t)(d.r * d.n * d.R);
+  xf_.ensure(nl, s_);
+  yf_.ensure(nl, s_);
+  w1f_.ensure(local_product_w1(d), s_);
+  w2f_.ensure(local_product_w2(d), s_);
+  op.lowp = true;
+  op.phi_l32 = phil32_.p;
+  op.A32 = A32_[k].p;
+  op.phi_r32 = phir32_.p;
+  op.xf = xf_.p;
+  op.yf = yf_.p;
+  op.w1f = w1f_.p;
+  op.w2f = w2f_.p;
+  lowp_count_ = 0;
+  op.count_lowp = &lowp_count_;
+}
+
+// Mixed-path rank search (same rule as amen_solve.h:385-403): the candidate of rank rr leaves out
+// the tail U[:, rr:] S Vh[rr:, :], so its residual is (B x - rhs) - B tail. The first term is the
+// FP64 residual of the solve; the tail is small near the truncation point, so its product with the
+// low-precision operator is accurate to the low-precision unit roundoff relative to ||B tail||.
+int AmenRun::rank_search_tail(const double* U, const double* SVh, int64_t a, int64_t bdim,
+                              int64_t kf, const double* resvec, double norm_rhs, double thr,
+                              const LocalOperator& op, int64_t nl, double* tail_buf) {
+  const int kChunk = 4;
+  int64_t r = kf;
+  DBuf y((size_t)nl, s_);
+  while (r > 0) {
+    const int64_t nc = r < kChunk ? r : kChunk;
+    for (int64_t c = 0; c < nc; ++c) {
+      const int64_t rr = r - c;
+      if (rr == kf) {
+        nrm2(red_, resvec, nl, slot(kCand + (int)c), s_);
+        continue;
+      }
+      ContractDesc cd;   // tail (a x b row-major) = U[:, rr:kf] SVh[rr:kf, :]
+      cd.M = (int)a; cd.N = (int)bdim; cd.K = (int)(kf - rr);
+      cd.A = U + rr * a; cd.am = Ax::one(1); cd.ak = Ax::one(a);
+      cd.B = SVh + rr; cd.bk = Ax::one(1); cd.bn = Ax::one(kf);
+      cd.C = tail_buf; cd.cm = Ax::one(bdim); cd.cn = Ax::one(1);
+      contract(cd, s_);
+      op.apply(tail_buf, y.p, false, s_);
+      sub(resvec, y.p, y.p, nl, s_);
+      nrm2(red_, y.p, nl, slot(kCand + (int)c), s_);
+    }
+    read_scalars(kCand + (int)nc);
+    for (int64_t c = 0; c < nc; ++c) {
+      const double res = hscal_[kCand + c] / norm_rhs;
+      if (res > thr) return (int)(r - c);
+    }
+    r -= nc;
+  }
+  return 0;
 }
 
 // z update after the local solve (amen_solve.h:418-442)
@@ -670,6 +809,7 @@ AmenResult AmenRun::run(const TTView& x0, const TTView& z0) {
     if (last) break;   // amen_solve.h:522-526
     if (max_res < p_.eps) last = true;
   }
+  phase(kPhOther);
   st_.sweeps = swp < p_.nswp ? swp + 1 : swp;
   st_.max_res = max_res;
   st_.converged = last ? 1 : 0;
@@ -683,6 +823,10 @@ AmenResult AmenRun::run(const TTView& x0, const TTView& z0) {
   }
   res.ranks = rx_;
   TTGB_CUDA(cudaStreamSynchronize(s_));
+  if (phases_) {
+    phases_->flush();
+    for (int i = 0; i < PhaseTimer::kPhases && i < 12; ++i) st_.phase_ms[i] = phases_->ms[i];
+  }
   if (prof_) {
     prof_->flush();
     st_.contract_ms = prof_->ms;

@@ -21,6 +21,12 @@ struct AmenParams {
   int prec = 0;
   uint64_t seed = 1;
   int profile = 0;   // time every local product / interface update with CUDA events
+  // 0: plain FP64 (the reference's arithmetic); 1: mixed - the local GMRES applies the operator
+  // with a low-precision contraction engine inside FP64 iterative refinement, and the rank search
+  // evaluates candidates as res - B tail (FP64 residual, low-precision product of the small tail).
+  int precision = 0;
+  int max_refine = 4;          // refinement steps per local solve (mixed)
+  double lowp_floor = 1e-5;    // relative target of one low-precision inner solve (mixed)
 };
 
 // A TT-matrix or TT-vector given by device pointers (borrowed).
@@ -44,6 +50,13 @@ struct AmenStats {
   int64_t direct_solves = 0;
   int64_t host_syncs = 0;
   int converged = 0;
+  int64_t lowp_matvecs = 0;       // low-precision local products (mixed path)
+  double lowp_flops = 0.0;        // their algorithmic flops
+  int64_t refinements = 0;        // FP64 refinement steps (mixed path)
+  // profile only: stream time per step of the sweep: backward z, backward QR, backward
+  // interfaces, forward setup, local solve, SVD, rank search, forward z, enrichment, forward
+  // interfaces, other
+  double phase_ms[12] = {0};
   // filled when AmenParams::profile is set: CUDA-event time of the contraction launches
   double contract_ms = 0.0;
   int64_t contract_launches = 0;

@@ -192,6 +192,13 @@ __global__ void fill_kernel(double* x, double v, int64_t n) {
     x[i] = v;
 }
 
+template <typename S, typename D>
+__global__ void cast_kernel(const S* __restrict__ x, D* y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (D)x[i];
+}
+
 __global__ void copy2d_kernel(const double* __restrict__ src, int64_t sld, double* dst, int64_t dld,
                               int64_t rows, int64_t cols) {
   const int64_t total = rows * cols;
@@ -331,6 +338,18 @@ void fill(double* x, double v, int64_t n, cudaStream_t s) {
 void copy(const double* x, double* y, int64_t n, cudaStream_t s) {
   if (n <= 0) return;
   TTGB_CUDA(cudaMemcpyAsync(y, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+}
+
+void cast(const double* x, float* y, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  cast_kernel<double, float><<<ew_grid(n), 256, 0, s>>>(x, y, n);
+  TTGB_CHECK_LAUNCH();
+}
+
+void cast(const float* x, double* y, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  cast_kernel<float, double><<<ew_grid(n), 256, 0, s>>>(x, y, n);
+  TTGB_CHECK_LAUNCH();
 }
 
 void copy2d(const double* src, int64_t sld, double* dst, int64_t dld, int64_t rows, int64_t cols,

@@ -44,6 +44,9 @@ void copy2d(const double* src, int64_t sld, double* dst, int64_t dld, int64_t ro
 // dst (rows x cols, row-major ld) = transpose of src (cols x rows, row-major sld)
 void transpose(const double* src, int64_t sld, double* dst, int64_t dld, int64_t rows, int64_t cols,
                cudaStream_t s);
+// precision casts
+void cast(const double* x, float* y, int64_t n, cudaStream_t s);
+void cast(const float* x, double* y, int64_t n, cudaStream_t s);
 // y = sum_i c[i] * Q_i (+ y0 if y0 != null), c device, Q_i = Q + i*ldq
 void combine(const double* Q, int64_t ldq, int k, const double* c, const double* y0, double* y,
              int64_t n, cudaStream_t s);

@@ -79,14 +79,23 @@ struct Scratch {   // per-call workspace of the kernel-level entry points
     red.cap_vec = 127;
     TTGB_CUDA(cudaMallocAsync((void**)&lws.status, 16, s));
     TTGB_CUDA(cudaMemsetAsync(lws.status, 0, 16, s));
-    TTGB_CUDA(cudaMallocHost((void**)&hbuf, 256));
+    hbuf = pinned_scratch();
     lws.h_status = (int*)hbuf;
   }
   ~Scratch() {
     cudaStreamSynchronize(s);
     if (counter) cudaFreeAsync(counter, s);
     if (lws.status) cudaFreeAsync(lws.status, s);
-    if (hbuf) cudaFreeHost(hbuf);
+  }
+  // one small pinned host buffer per host thread, kept for the thread's lifetime
+  static char* pinned_scratch() {
+    struct Holder {
+      char* p = nullptr;
+      ~Holder() { if (p) cudaFreeHost(p); }
+    };
+    static thread_local Holder h;
+    if (!h.p) TTGB_CUDA(cudaMallocHost((void**)&h.p, 256));
+    return h.p;
   }
 };
 
@@ -112,6 +121,7 @@ void ttgb_default_params(ttgb_amen_params* p) {
   p->preconditioner = TTGB_PREC_NONE;
   p->seed = 1;
   p->profile = 0;
+  p->precision = TTGB_PRECISION_FP64;
 }
 
 int ttgb_amen_solve(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, const ttgb_tt* z0,
@@ -133,6 +143,9 @@ int ttgb_amen_solve(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, const
     p.prec = params->preconditioner;
     p.seed = params->seed;
     p.profile = params->profile;
+    TTGB_REQUIRE(params->precision == TTGB_PRECISION_FP64 || params->precision == TTGB_PRECISION_MIXED,
+                 "invalid precision mode");
+    p.precision = params->precision;
     auto* sol = new ttgb_solution;
     try {
       sol->res = amen_solve(Av, bv, xv, zv, p, as_stream(stream));
@@ -171,6 +184,10 @@ int ttgb_solution_stats(const ttgb_solution* sol, ttgb_stats* st) {
     st->contract_ms = a.contract_ms;
     st->contract_launches = a.contract_launches;
     st->contract_flops = a.contract_flops;
+    st->lowp_matvecs = a.lowp_matvecs;
+    st->lowp_flops = a.lowp_flops;
+    st->refinements = a.refinements;
+    for (int i = 0; i < 12; ++i) st->phase_ms[i] = a.phase_ms[i];
   });
 }
 

@@ -70,20 +70,21 @@ inline int num_sms() {
 
 inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
 
-// A stream-ordered FP64 device buffer (cudaMallocAsync / cudaFreeAsync from the device's default
-// memory pool, whose release threshold the context raises so that freed blocks are reused).
-struct DBuf {
-  double* p = nullptr;
+// A stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync from the device's default
+// memory pool, whose release threshold the solver raises so that freed blocks are reused).
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
   size_t n = 0;
   cudaStream_t s = nullptr;
 
-  DBuf() = default;
-  DBuf(size_t count, cudaStream_t stream) { reset(count, stream); }
-  ~DBuf() { release(); }
-  DBuf(const DBuf&) = delete;
-  DBuf& operator=(const DBuf&) = delete;
-  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
-  DBuf& operator=(DBuf&& o) noexcept {
+  DevBuf() = default;
+  DevBuf(size_t count, cudaStream_t stream) { reset(count, stream); }
+  ~DevBuf() { release(); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
     if (this != &o) {
       release();
       p = o.p; n = o.n; s = o.s;
@@ -95,7 +96,7 @@ struct DBuf {
     release();
     s = stream;
     n = count;
-    if (count) TTGB_CUDA(cudaMallocAsync((void**)&p, count * sizeof(double), stream));
+    if (count) TTGB_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), stream));
   }
   // grow-only reuse: keeps the allocation when it is already large enough
   void ensure(size_t count, cudaStream_t stream) {
@@ -106,8 +107,10 @@ struct DBuf {
     p = nullptr;
     n = 0;
   }
-  double* get() const { return p; }
+  T* get() const { return p; }
 };
+using DBuf = DevBuf<double>;
+using FBuf = DevBuf<float>;
 
 // A dense tensor in device memory: buffer plus its dims (row-major, last dim fastest).
 struct DTensor {

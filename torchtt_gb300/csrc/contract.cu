@@ -25,28 +25,29 @@ __device__ __forceinline__ int64_t ax_off(const AxD& a, int i) {
   return (int64_t)i1 * a.s1 + (int64_t)i0 * a.s0;
 }
 
+template <typename T>
 struct KParams {
   int M, N, K, batch, splitk, kchunk;
-  const double* A;
+  const T* A;
   AxD am, ak;
   int64_t a_bs;
-  const double* B;
+  const T* B;
   AxD bk, bn;
   int64_t b_bs;
-  double* C;
+  T* C;
   AxD cm, cn;
   int64_t c_bs;
-  double alpha, beta;
+  T alpha, beta;
 };
 
 constexpr int BK = 16;
 constexpr int NT = 256;
 
-template <int BM, int BN>
-__global__ void __launch_bounds__(NT) contract_kernel(KParams p) {
+template <typename T, int BM, int BN>
+__global__ void __launch_bounds__(NT) contract_kernel(KParams<T> p) {
   constexpr int TM = BM / 16, TN = BN / 16;
-  __shared__ double As[BK][BM + 1];
-  __shared__ double Bs[BK][BN + 1];
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
 
   const int tid = threadIdx.x;
   const int bz = blockIdx.z;
@@ -56,8 +57,8 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams p) {
   const int kend = min(p.K, kbeg + p.kchunk);
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
 
-  const double* A = p.A + (int64_t)bidx * p.a_bs;
-  const double* B = p.B + (int64_t)bidx * p.b_bs;
+  const T* A = p.A + (int64_t)bidx * p.a_bs;
+  const T* B = p.B + (int64_t)bidx * p.b_bs;
 
   // loader mapping: A tile BM x BK, B tile BK x BN, NT threads
   constexpr int A_ROWS_PER_PASS = NT / BK;   // threads cover (row, k) with k = tid % BK
@@ -83,11 +84,11 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams p) {
   }
 
   const int ty = tid / 16, tx = tid % 16;
-  double acc[TM][TN];
+  T acc[TM][TN];
 #pragma unroll
   for (int i = 0; i < TM; ++i)
 #pragma unroll
-    for (int j = 0; j < TN; ++j) acc[i][j] = 0.0;
+    for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
 
   for (int k0 = kbeg; k0 < kend; k0 += BK) {
     const int k = k0 + lk;
@@ -96,14 +97,14 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams p) {
     const int64_t b_koff = kok ? ax_off(p.bk, k) : 0;
 #pragma unroll
     for (int i = 0; i < BM / A_ROWS_PER_PASS; ++i)
-      As[lk][lr + i * A_ROWS_PER_PASS] = (kok && a_mok[i]) ? __ldg(A + a_moff[i] + a_koff) : 0.0;
+      As[lk][lr + i * A_ROWS_PER_PASS] = (kok && a_mok[i]) ? __ldg(A + a_moff[i] + a_koff) : T(0);
 #pragma unroll
     for (int i = 0; i < BN / B_COLS_PER_PASS; ++i)
-      Bs[lk][lr + i * B_COLS_PER_PASS] = (kok && b_nok[i]) ? __ldg(B + b_noff[i] + b_koff) : 0.0;
+      Bs[lk][lr + i * B_COLS_PER_PASS] = (kok && b_nok[i]) ? __ldg(B + b_noff[i] + b_koff) : T(0);
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
-      double a[TM], b[TN];
+      T a[TM], b[TN];
 #pragma unroll
       for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + 16 * i];
 #pragma unroll
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams p) {
     __syncthreads();
   }
 
-  double* C = p.C + (int64_t)bidx * p.c_bs;
+  T* C = p.C + (int64_t)bidx * p.c_bs;
 #pragma unroll
   for (int i = 0; i < TM; ++i) {
     const int m = m0 + ty + 16 * i;
@@ -126,28 +127,29 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams p) {
     for (int j = 0; j < TN; ++j) {
       const int n = n0 + tx + 16 * j;
       if (n >= p.N) continue;
-      double* c = C + cmo + ax_off(p.cn, n);
-      const double v = p.alpha * acc[i][j];
+      T* c = C + cmo + ax_off(p.cn, n);
+      const T v = p.alpha * acc[i][j];
       if (p.splitk > 1) {
         atomicAdd(c, v);
       } else {
-        *c = (p.beta == 0.0) ? v : fma(p.beta, *c, v);
+        *c = (p.beta == T(0)) ? v : fma(p.beta, *c, v);
       }
     }
   }
 }
 
 // C <- beta * C over the (batched, strided) output index space
-__global__ void scale_output_kernel(double* C, int M, int N, int batch, AxD cm, AxD cn, int64_t c_bs,
-                                    double beta) {
+template <typename T>
+__global__ void scale_output_kernel(T* C, int M, int N, int batch, AxD cm, AxD cn, int64_t c_bs,
+                                    T beta) {
   const int64_t total = (int64_t)M * N * batch;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x) {
     int b = (int)(t / ((int64_t)M * N));
     int rem = (int)(t - (int64_t)b * M * N);
     int m = rem / N, n = rem - (rem / N) * N;
-    double* c = C + (int64_t)b * c_bs + ax_off(cm, m) + ax_off(cn, n);
-    *c = (beta == 0.0) ? 0.0 : beta * *c;
+    T* c = C + (int64_t)b * c_bs + ax_off(cm, m) + ax_off(cn, n);
+    *c = (beta == T(0)) ? T(0) : beta * *c;
   }
 }
 
@@ -164,11 +166,10 @@ AxD to_dev(const Ax& a, int extent) {
   return r;
 }
 
-}  // namespace
-
-void contract(const ContractDesc& d, cudaStream_t stream, bool deterministic) {
+template <typename T>
+void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool deterministic) {
   if (d.M <= 0 || d.N <= 0 || d.batch <= 0) return;
-  KParams p;
+  KParams<T> p;
   p.M = d.M; p.N = d.N; p.K = d.K; p.batch = d.batch;
   p.A = d.A; p.am = to_dev(d.am, d.M); p.ak = to_dev(d.ak, d.K); p.a_bs = d.a_bs;
   p.B = d.B; p.bk = to_dev(d.bk, d.K); p.bn = to_dev(d.bn, d.N); p.b_bs = d.b_bs;
@@ -212,23 +213,33 @@ void contract(const ContractDesc& d, cudaStream_t stream, bool deterministic) {
   }
   dim3 grid(cdiv(d.N, bn), cdiv(d.M, bm), (unsigned)(d.batch * splitk));
   TTGB_REQUIRE(grid.y < 65536 && grid.z < 65536, "contraction grid too large");
-  if (bm == 64 && bn == 64) contract_kernel<64, 64><<<grid, NT, 0, stream>>>(p);
-  else if (bm == 64 && bn == 32) contract_kernel<64, 32><<<grid, NT, 0, stream>>>(p);
-  else if (bm == 32 && bn == 64) contract_kernel<32, 64><<<grid, NT, 0, stream>>>(p);
-  else contract_kernel<32, 32><<<grid, NT, 0, stream>>>(p);
+  if (bm == 64 && bn == 64) contract_kernel<T, 64, 64><<<grid, NT, 0, stream>>>(p);
+  else if (bm == 64 && bn == 32) contract_kernel<T, 64, 32><<<grid, NT, 0, stream>>>(p);
+  else if (bm == 32 && bn == 64) contract_kernel<T, 32, 64><<<grid, NT, 0, stream>>>(p);
+  else contract_kernel<T, 32, 32><<<grid, NT, 0, stream>>>(p);
   TTGB_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+void contract(const ContractDesc& d, cudaStream_t stream, bool deterministic) {
+  launch_contract<double>(d, stream, deterministic);
+}
+
+void contract(const ContractDescF& d, cudaStream_t stream, bool deterministic) {
+  launch_contract<float>(d, stream, deterministic);
 }
 
 // --------------------------------------------------------------------------------------------
 // AMEn contraction recipes
 // --------------------------------------------------------------------------------------------
 
-void local_product(const LocalOpDims& d, const double* phi_l, const double* A, const double* phi_r,
-                   const double* x, double* y, double* w1, double* w2, cudaStream_t stream,
-                   double alpha, double beta) {
+template <typename T>
+static void local_product_t(const LocalOpDims& d, const T* phi_l, const T* A, const T* phi_r,
+                            const T* x, T* y, T* w1, T* w2, cudaStream_t stream, T alpha, T beta) {
   // step 1: W[(l,s),(n,R)] = sum_r Phi_l[(l,s), r] X[r, (n,R)]
   {
-    ContractDesc c;
+    ContractDescT<T> c;
     c.M = (int)(d.rl * d.s); c.N = (int)(d.n * d.R); c.K = (int)d.r;
     c.A = phi_l; c.am = Ax::one(d.r); c.ak = Ax::one(1);
     c.B = x; c.bk = Ax::one(d.n * d.R); c.bn = Ax::one(1);
@@ -237,7 +248,7 @@ void local_product(const LocalOpDims& d, const double* phi_l, const double* A, c
   }
   // step 2 (batched over l): Y2_l[(m,S), R] = sum_{(s,n)} A[s,m,n,S] W_l[(s,n), R]
   {
-    ContractDesc c;
+    ContractDescT<T> c;
     c.M = (int)(d.m * d.S); c.N = (int)d.R; c.K = (int)(d.s * d.n); c.batch = (int)d.rl;
     c.A = A; c.am = Ax::two(d.S, d.n * d.S, 1); c.ak = Ax::two(d.n, d.m * d.n * d.S, d.S);
     c.B = w1; c.bk = Ax::one(d.R); c.bn = Ax::one(1); c.b_bs = d.s * d.n * d.R;
@@ -246,7 +257,7 @@ void local_product(const LocalOpDims& d, const double* phi_l, const double* A, c
   }
   // step 3: y[(l,m), L] = alpha * sum_{(S,R)} Y2[(l,m),(S,R)] Phi_r[L,(S,R)] + beta * y
   {
-    ContractDesc c;
+    ContractDescT<T> c;
     c.M = (int)(d.rl * d.m); c.N = (int)d.RL; c.K = (int)(d.S * d.R);
     c.A = w2; c.am = Ax::one(d.S * d.R); c.ak = Ax::one(1);
     c.B = phi_r; c.bk = Ax::one(1); c.bn = Ax::one(d.S * d.R);
@@ -254,6 +265,18 @@ void local_product(const LocalOpDims& d, const double* phi_l, const double* A, c
     c.alpha = alpha; c.beta = beta;
     contract(c, stream);
   }
+}
+
+void local_product(const LocalOpDims& d, const double* phi_l, const double* A, const double* phi_r,
+                   const double* x, double* y, double* w1, double* w2, cudaStream_t stream,
+                   double alpha, double beta) {
+  local_product_t<double>(d, phi_l, A, phi_r, x, y, w1, w2, stream, alpha, beta);
+}
+
+void local_product(const LocalOpDims& d, const float* phi_l, const float* A, const float* phi_r,
+                   const float* x, float* y, float* w1, float* w2, cudaStream_t stream,
+                   float alpha, float beta) {
+  local_product_t<float>(d, phi_l, A, phi_r, x, y, w1, w2, stream, alpha, beta);
 }
 
 size_t phi_A_workspace(const PhiDims& d) {

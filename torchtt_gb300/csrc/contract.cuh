@@ -18,23 +18,28 @@ struct Ax {
 };
 
 // C[b](m, n) = alpha * sum_k A[b](m, k) * B[b](k, n) + beta * C[b](m, n)
-struct ContractDesc {
+template <typename T>
+struct ContractDescT {
   int M = 0, N = 0, K = 0, batch = 1;
-  const double* A = nullptr;
+  const T* A = nullptr;
   Ax am, ak;
   int64_t a_bs = 0;
-  const double* B = nullptr;
+  const T* B = nullptr;
   Ax bk, bn;
   int64_t b_bs = 0;
-  double* C = nullptr;
+  T* C = nullptr;
   Ax cm, cn;
   int64_t c_bs = 0;
-  double alpha = 1.0, beta = 0.0;
+  T alpha = T(1), beta = T(0);
 };
+using ContractDesc = ContractDescT<double>;
+using ContractDescF = ContractDescT<float>;
 
 // Launches the contraction on `stream`. Picks a split-K factor when the output has too few tiles
 // to fill the GPU (then C is pre-scaled by beta and partial sums are added atomically).
 void contract(const ContractDesc& d, cudaStream_t stream, bool deterministic = false);
+// The same engine in FP32 (CUDA-core FFMA), for the low-precision local operator.
+void contract(const ContractDescF& d, cudaStream_t stream, bool deterministic = false);
 
 // Local AMEn product y[l,m,L] = sum Phi_left[l,s,r] A[s,m,n,S] Phi_right[L,S,R] x[r,n,R]
 // (reference: local_product, cpp/amen_solve.h:17-27). `w1` needs r_l*s*n*R and `w2` r_l*m*S*R
@@ -48,6 +53,9 @@ struct LocalOpDims {
 void local_product(const LocalOpDims& d, const double* phi_l, const double* A, const double* phi_r,
                    const double* x, double* y, double* w1, double* w2, cudaStream_t stream,
                    double alpha = 1.0, double beta = 0.0);
+void local_product(const LocalOpDims& d, const float* phi_l, const float* A, const float* phi_r,
+                   const float* x, float* y, float* w1, float* w2, cudaStream_t stream,
+                   float alpha = 1.0f, float beta = 0.0f);
 inline size_t local_product_w1(const LocalOpDims& d) { return size_t(d.rl * d.s * d.n * d.R); }
 inline size_t local_product_w2(const LocalOpDims& d) { return size_t(d.rl * d.m * d.S * d.R); }
 

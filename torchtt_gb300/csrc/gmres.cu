@@ -13,8 +13,22 @@ void LocalOperator::apply(const double* x, double* y, bool use_prec, cudaStream_
     apply_prec(x, wp, s);
     in = wp;
   }
+  if (lowp) {
+    cast(in, xf, size(), s);
+    local_product(dims, phi_l32, A32, phi_r32, xf, yf, w1f, w2f, s);
+    cast(yf, y, dims.rl * dims.m * dims.RL, s);
+    if (count_lowp) ++*count_lowp;
+    return;
+  }
   if (prof) prof->begin();
   local_product(dims, phi_l, A, phi_r, in, y, w1, w2, s);
+  if (prof) prof->end(local_product_flops(dims), 3);
+  if (count) ++*count;
+}
+
+void LocalOperator::apply_fp64(const double* x, double* y, cudaStream_t s) const {
+  if (prof) prof->begin();
+  local_product(dims, phi_l, A, phi_r, x, y, w1, w2, s);
   if (prof) prof->end(local_product_flops(dims), 3);
   if (count) ++*count;
 }

@@ -30,8 +30,21 @@ struct LocalOperator {
   double* wp = nullptr;         // preconditioned input (N_loc)
   Profiler* prof = nullptr;     // optional launch timing
   int64_t* count = nullptr;     // optional: incremented per application
+  // Low-precision engine (mixed path): when lowp is set, apply() runs the contraction in FP32 on
+  // FP32 copies of the operator (phi_l32, A32, phi_r32) and converts the vector in and out;
+  // apply_fp64() always uses the FP64 operator (true residuals).
+  bool lowp = false;
+  const float* phi_l32 = nullptr;
+  const float* A32 = nullptr;
+  const float* phi_r32 = nullptr;
+  float* xf = nullptr;          // N_loc
+  float* yf = nullptr;          // N_loc
+  float* w1f = nullptr;
+  float* w2f = nullptr;
+  int64_t* count_lowp = nullptr;
   int64_t size() const { return dims.r * dims.n * dims.R; }
   void apply(const double* x, double* y, bool use_prec, cudaStream_t s) const;
+  void apply_fp64(const double* x, double* y, cudaStream_t s) const;
   void apply_prec(const double* x, double* y, cudaStream_t s) const;
 };
 

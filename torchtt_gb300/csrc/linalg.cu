@@ -4,10 +4,14 @@
 // GB300 note: FP64 runs at ~1.9 FMA/clock/SM (measured), so every O(m n^2) step is expressed as a
 // GEMM on the contraction engine (spread over all SMs); only O(n^3) steps on the small n x n
 // factors (Cholesky, triangular inverse, Jacobi) run inside one thread block.
+#include <cooperative_groups.h>
+
 #include <cmath>
 
 #include "contract.cuh"
 #include "linalg.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace ttgb {
 
@@ -101,6 +105,104 @@ __global__ void __launch_bounds__(512) chol_kernel(double* G, int n, int64_t shi
   for (int64_t t = tid; t < (int64_t)n * n; t += nt) {
     const int i = (int)(t / n), k = (int)(t % n);
     if (k < i) G[t] = 0.0;
+  }
+}
+
+// Fused, shared-memory resident Cholesky + triangular inverse for n <= kCholSmemMax:
+// G (row-major, global) -> R (upper, G = R^T R) written to Rout, Ri = R^{-1} written to Riout.
+// Same shift / identity check semantics as chol_kernel. One block; both n x n factors live in
+// shared memory, so every step is a shared-memory FP64 update plus one barrier.
+constexpr int kCholSmemMax = 112;
+
+__global__ void __launch_bounds__(512) chol_inv_smem_kernel(const double* __restrict__ Gin, int n,
+                                                            int64_t shift_rows, int check_identity,
+                                                            double* Rout, double* Riout, int* status) {
+  extern __shared__ double sm[];
+  const int ld = n + 1;   // padded rows
+  double* G = sm;                 // becomes R (upper)
+  double* X = sm + n * ld;        // becomes R^{-1} (upper)
+  __shared__ double sh[32];
+  __shared__ int bad;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int t = tid; t < n * n; t += nt) G[(t / n) * ld + (t % n)] = Gin[t];
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  if (check_identity) {
+    double mx = 0.0;
+    for (int t = tid; t < n * n; t += nt) {
+      const int i = t / n, k = t % n;
+      const double v = G[i * ld + k] - (i == k ? 1.0 : 0.0);
+      mx = fmax(mx, isfinite(v) ? fabs(v) : 1e300);
+    }
+    mx = block_max_d(mx, sh);
+    if (tid == 0 && !(mx <= 0.1)) *status = 2;
+  }
+  if (shift_rows > 0) {
+    double tr = 0.0;
+    for (int i = tid; i < n; i += nt) tr += G[i * ld + i];
+    tr = block_sum_d(tr, sh);
+    const double sft = 11.0 * ((double)shift_rows * n + (double)n * (n + 1)) * kEps * tr;
+    for (int i = tid; i < n; i += nt) G[i * ld + i] += sft;
+  }
+  __syncthreads();
+  // right-looking Cholesky, upper triangle only
+  for (int j = 0; j < n; ++j) {
+    const double d = G[j * ld + j];
+    if (!(d > 0.0) || !isfinite(d)) {
+      if (tid == 0) { bad = 1; *status = 1; }
+    }
+    __syncthreads();
+    if (bad) break;
+    const double rd = sqrt(d);
+    const double inv = 1.0 / rd;
+    for (int k = j + 1 + tid; k < n; k += nt) G[j * ld + k] *= inv;
+    __syncthreads();
+    if (tid == 0) G[j * ld + j] = rd;
+    {   // trailing update of the upper triangle: one warp per row, lanes over columns
+      const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+      for (int i = j + 1 + warp; i < n; i += nw) {
+        const double gji = G[j * ld + i];
+        double* gi = G + i * ld;
+        const double* gj = G + j * ld;
+        for (int k = i + lane; k < n; k += 32) gi[k] = fma(-gji, gj[k], gi[k]);
+      }
+    }
+    __syncthreads();
+  }
+  if (bad) return;
+  {
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    for (int i = warp; i < n; i += nw)
+      for (int k = lane; k < n; k += 32) {
+        if (k < i) G[i * ld + k] = 0.0;
+        X[i * ld + k] = (k == i) ? 1.0 : 0.0;
+      }
+  }
+  __syncthreads();
+  // X = R^{-1} by column-oriented back substitution on the identity: for j = n-1..0 the row j of
+  // X is final after scaling, then its multiples are removed from the rows above (one warp per row).
+  {
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    for (int j = n - 1; j >= 0; --j) {
+      const double inv = 1.0 / G[j * ld + j];
+      for (int k = j + tid; k < n; k += nt) X[j * ld + k] *= inv;
+      __syncthreads();
+      for (int i = warp; i < j; i += nw) {
+        const double gij = G[i * ld + j];
+        double* xi = X + i * ld;
+        const double* xj = X + j * ld;
+        for (int k = j + lane; k < n; k += 32) xi[k] = fma(-gij, xj[k], xi[k]);
+      }
+      __syncthreads();
+    }
+  }
+  {
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    for (int i = warp; i < n; i += nw)
+      for (int k = lane; k < n; k += 32) {
+        Rout[i * n + k] = G[i * ld + k];
+        Riout[i * n + k] = X[i * ld + k];
+      }
   }
 }
 
@@ -200,7 +302,7 @@ __device__ __forceinline__ int rr_index(int p, int r, int nn) {
 
 __global__ void __launch_bounds__(512) jacobi_svd_kernel(double* Wg, double* Vg, int n, double* U,
                                                          double* S, int use_smem, int max_sweeps,
-                                                         int* status) {
+                                                         int* status, const double* Vinit) {
   extern __shared__ double smem[];
   __shared__ int nrot;
   double* W = use_smem ? smem : Wg;
@@ -210,7 +312,8 @@ __global__ void __launch_bounds__(512) jacobi_svd_kernel(double* Wg, double* Vg,
   if (use_smem) {
     for (int64_t t = tid; t < (int64_t)n * n; t += nt) W[t] = Wg[t];
   }
-  for (int64_t t = tid; t < (int64_t)n * n; t += nt) V[t] = ((t % n) == (t / n)) ? 1.0 : 0.0;
+  for (int64_t t = tid; t < (int64_t)n * n; t += nt)
+    V[t] = Vinit ? Vinit[t] : (((t % n) == (t / n)) ? 1.0 : 0.0);
   __syncthreads();
   const int nn = n + (n & 1);
   const double tol = fmax((double)n, 1.0) * kEps;
@@ -301,6 +404,139 @@ __global__ void __launch_bounds__(512) jacobi_svd_kernel(double* Wg, double* Vg,
   }
   __syncthreads();
   for (int64_t t = tid; t < (int64_t)n * n; t += nt) Vg[t] = Vg[(int64_t)n * n + t];
+}
+
+// ---------------------------------------------------------------------------------------------
+// One-sided Jacobi on a thread-block cluster: the FP64 work of a sweep is spread over
+// kJacobiCluster SMs. Column j of W and of V lives in the shared memory of CTA j % C (slot j / C);
+// in every round of the round-robin ordering each CTA's warps rotate their share of the n/2
+// disjoint pairs, reading and writing partner columns through distributed shared memory, and one
+// cluster barrier separates rounds. The sweep count is summed in CTA 0 after a barrier and read by
+// every CTA after another, so all CTAs leave the loop together.
+// ---------------------------------------------------------------------------------------------
+constexpr int kJacobiCluster = 8;
+constexpr int kJacobiClusterMaxN = 320;   // 2 ceil(n/8) n doubles of shared memory per CTA
+
+__global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
+    jacobi_cluster_kernel(const double* __restrict__ Win, int n, double* Wout, double* Vout,
+                          int max_sweeps, int* status) {
+  extern __shared__ double sm[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = kJacobiCluster;
+  const int rank = (int)cluster.block_rank();
+  const int ncl = (n + C - 1) / C;
+  double* Wl = sm;
+  double* Vl = sm + (int64_t)ncl * n;
+  __shared__ int counts[kJacobiCluster];   // CTA 0's copy collects the per-CTA rotation counts
+  __shared__ int local_cnt;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int t = 0; t < ncl; ++t) {
+    const int j = rank + C * t;
+    for (int i = tid; i < n; i += nt) {
+      Wl[(int64_t)t * n + i] = (j < n) ? Win[(int64_t)j * n + i] : 0.0;
+      Vl[(int64_t)t * n + i] = (j < n && i == j) ? 1.0 : 0.0;
+    }
+  }
+  int* counts0 = cluster.map_shared_rank(counts, 0);
+  const int nn = n + (n & 1);
+  const double tol = fmax((double)n, 1.0) * kEps;
+  int sweep = 0;
+  bool converged = false;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (tid == 0) local_cnt = 0;
+    cluster.sync();
+    int mine = 0;
+    for (int r = 0; r < nn - 1; ++r) {
+      for (int pi = rank + C * warp; pi < nn / 2; pi += C * nw) {
+        int p = rr_index(pi, r, nn), q = rr_index(nn - 1 - pi, r, nn);
+        if (p > q) { const int t = p; p = q; q = t; }
+        if (q >= n) continue;
+        double* wp = cluster.map_shared_rank(Wl + (int64_t)(p / C) * n, p % C);
+        double* wq = cluster.map_shared_rank(Wl + (int64_t)(q / C) * n, q % C);
+        double a = 0.0, b = 0.0, g = 0.0;
+        for (int i = lane; i < n; i += 32) {
+          const double x = wp[i], y = wq[i];
+          a = fma(x, x, a); b = fma(y, y, b); g = fma(x, y, g);
+        }
+        a = warp_sum_d(a); b = warp_sum_d(b); g = warp_sum_d(g);
+        if (a == 0.0 || b == 0.0) continue;
+        if (!(fabs(g) > tol * sqrt(a) * sqrt(b))) continue;
+        const double zeta = (b - a) / (2.0 * g);
+        const double t = (fabs(zeta) > 1e150) ? 0.5 / zeta
+                                               : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+        for (int i = lane; i < n; i += 32) {
+          const double x = wp[i], y = wq[i];
+          wp[i] = c * x - s * y;
+          wq[i] = s * x + c * y;
+        }
+        double* vp = cluster.map_shared_rank(Vl + (int64_t)(p / C) * n, p % C);
+        double* vq = cluster.map_shared_rank(Vl + (int64_t)(q / C) * n, q % C);
+        for (int i = lane; i < n; i += 32) {
+          const double x = vp[i], y = vq[i];
+          vp[i] = c * x - s * y;
+          vq[i] = s * x + c * y;
+        }
+        ++mine;
+      }
+      cluster.sync();
+    }
+    if (lane == 0 && mine) atomicAdd(&local_cnt, mine);
+    __syncthreads();
+    if (tid == 0) counts0[rank] = local_cnt;
+    cluster.sync();
+    int total = 0;
+    for (int c = 0; c < C; ++c) total += counts0[c];
+    cluster.sync();
+    if (total == 0) { converged = true; break; }
+  }
+  if (rank == 0 && tid == 0 && !converged) *status = 3;
+  for (int t = 0; t < ncl; ++t) {
+    const int j = rank + C * t;
+    if (j >= n) break;
+    for (int i = tid; i < n; i += nt) {
+      Wout[(int64_t)j * n + i] = Wl[(int64_t)t * n + i];
+      Vout[(int64_t)j * n + i] = Vl[(int64_t)t * n + i];
+    }
+  }
+}
+
+// From the rotated W (column-major n x n) and the rotations V: sigma_j = ||W_j||, descending order;
+// Un[:, rank_j] = W_j / sigma_j, Vs[:, rank_j] = V_j, S[rank_j] = sigma_j. One block.
+__global__ void __launch_bounds__(1024) svd_sort_kernel(const double* __restrict__ W,
+                                                        const double* __restrict__ V, int n,
+                                                        double* Un, double* S, double* Vs,
+                                                        double* sig) {
+  __shared__ int rank_sh[1024];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int j = warp; j < n; j += nw) {
+    double a = 0.0;
+    for (int i = lane; i < n; i += 32) a = fma(W[(int64_t)j * n + i], W[(int64_t)j * n + i], a);
+    a = warp_sum_d(a);
+    if (lane == 0) sig[j] = sqrt(a);
+  }
+  __syncthreads();
+  for (int j = tid; j < n; j += nt) {
+    const double sj = sig[j];
+    int rk = 0;
+    for (int i = 0; i < n; ++i) {
+      const double si = sig[i];
+      rk += (si > sj) || (si == sj && i < j);
+    }
+    rank_sh[j] = rk;
+  }
+  __syncthreads();
+  for (int j = tid; j < n; j += nt) S[rank_sh[j]] = sig[j];
+  for (int j = warp; j < n; j += nw) {
+    const int rk = rank_sh[j];
+    const double inv = sig[j] > 0.0 ? 1.0 / sig[j] : 0.0;
+    for (int i = lane; i < n; i += 32) {
+      Un[(int64_t)rk * n + i] = W[(int64_t)j * n + i] * inv;
+      Vs[(int64_t)rk * n + i] = V[(int64_t)j * n + i];
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -461,10 +697,19 @@ QRResult qr(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, doubl
   double* outs[3] = {Q, Qt, Q};
   for (int pass = 0; pass < 3; ++pass) {
     gemm_cm(Ain, ldin, Ain, ldin, G, n, n, n, m, 1.0, 0.0, s, true, false);
-    chol_kernel<<<1, 512, 0, s>>>(G, (int)n, pass == 0 ? m : 0, pass == 2 ? 1 : 0, ws.status);
-    TTGB_CHECK_LAUNCH();
-    trinv_kernel<<<cdiv(n, 128), 128, 0, s>>>(G, Ri, (int)n);
-    TTGB_CHECK_LAUNCH();
+    if (n <= kCholSmemMax) {
+      const size_t smem = (size_t)2 * n * (n + 1) * sizeof(double);
+      TTGB_CUDA(cudaFuncSetAttribute(chol_inv_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(2 * kCholSmemMax * (kCholSmemMax + 1) * sizeof(double))));
+      chol_inv_smem_kernel<<<1, 512, smem, s>>>(G, (int)n, pass == 0 ? m : 0, pass == 2 ? 1 : 0, G,
+                                                Ri, ws.status);
+      TTGB_CHECK_LAUNCH();
+    } else {
+      chol_kernel<<<1, 512, 0, s>>>(G, (int)n, pass == 0 ? m : 0, pass == 2 ? 1 : 0, ws.status);
+      TTGB_CHECK_LAUNCH();
+      trinv_kernel<<<cdiv(n, 128), 128, 0, s>>>(G, Ri, (int)n);
+      TTGB_CHECK_LAUNCH();
+    }
     // Q_next = Ain * R^{-1}   (Ri row-major == (Ri)^T column-major)
     gemm_cm(Ain, ldin, Ri, n, outs[pass], m, m, n, n, 1.0, 0.0, s, false, true);
     if (pass == 0) {
@@ -502,28 +747,44 @@ void svd(const double* A, int64_t lda, int64_t m, int64_t n, double* U, double* 
     transpose(Ut.p, n, Vh, m, n, m, s);
     return;
   }
-  // m >= n: A = Q R, R = Ur S V^T
+  // m >= n: A = Q R; one-sided Jacobi on R^T (QR-preconditioned Jacobi, Drmac & Veselic, SIAM J.
+  // Matrix Anal. Appl. 29, 2008): R^T = U' S V'^T converges in far fewer sweeps than Jacobi on R.
+  // Then R = V' S U'^T and A = (Q V') S U'^T.
   DBuf Qb((size_t)(m * n), s), Rb((size_t)(n * n), s);
   qr(A, lda, m, n, Qb.p, Rb.p, ws, red, s);
+  TTGB_REQUIRE(n <= 1024, "SVD: too many columns");
   ws.c.ensure(3 * n * n + 16, s);
-  double* W = ws.c.p;        // n x n working copy of R
-  double* Vw = W + n * n;    // 2 n x n: V and scratch
-  copy(Rb.p, W, n * n, s);
-  DBuf Ur((size_t)(n * n), s);
+  double* W = ws.c.p;        // n x n: R^T, rotated in place
+  double* Vw = W + n * n;    // 2 n x n: accumulated rotations V' (sorted) and scratch
+  transpose(Rb.p, n, W, n, n, n, s);
+  DBuf Up((size_t)(n * n), s);   // U' (normalised columns of the rotated R^T, sorted)
+  if (n <= kJacobiClusterMaxN && n >= 2 * kJacobiCluster) {
+    const int ncl = (int)((n + kJacobiCluster - 1) / kJacobiCluster);
+    const size_t smem = (size_t)2 * ncl * n * sizeof(double);
+    TTGB_CUDA(cudaFuncSetAttribute(jacobi_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+    jacobi_cluster_kernel<<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status);
+    TTGB_CHECK_LAUNCH();
+    DBuf sig((size_t)n, s);
+    svd_sort_kernel<<<1, 1024, 0, s>>>(W, Vw, (int)n, Up.p, S, Vw + n * n, sig.p);
+    TTGB_CHECK_LAUNCH();
+    gemm_cm(Qb.p, m, Vw + n * n, n, U, m, m, n, n, 1.0, 0.0, s);   // U = Q V'
+    transpose(Up.p, n, Vh, n, n, n, s);                            // Vh = U'^T
+    return;
+  }
   const size_t smem = (size_t)2 * n * n * sizeof(double);
   const int use_smem = smem <= 200 * 1024 ? 1 : 0;
   if (use_smem) {
     TTGB_CUDA(cudaFuncSetAttribute(jacobi_svd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
   }
-  TTGB_REQUIRE(n <= 1024, "SVD: too many columns");
-  jacobi_svd_kernel<<<1, 512, use_smem ? smem : 0, s>>>(W, Vw, (int)n, Ur.p, S, use_smem, 60,
-                                                         ws.status);
+  jacobi_svd_kernel<<<1, 512, use_smem ? smem : 0, s>>>(W, Vw, (int)n, Up.p, S, use_smem, 60,
+                                                         ws.status, nullptr);
   TTGB_CHECK_LAUNCH();
-  // U = Q Ur
-  gemm_cm(Qb.p, m, Ur.p, n, U, m, m, n, n, 1.0, 0.0, s);
-  // Vh (n x n col-major) = V^T
-  transpose(Vw, n, Vh, n, n, n, s);
+  // U = Q V'
+  gemm_cm(Qb.p, m, Vw, n, U, m, m, n, n, 1.0, 0.0, s);
+  // Vh (n x n col-major) = U'^T
+  transpose(Up.p, n, Vh, n, n, n, s);
 }
 
 void lu_solve(const double* B, int64_t n, const double* rhs, double* x, LinalgWS& ws,

@@ -55,4 +55,49 @@ struct Profiler {
   }
 };
 
+// Attribution of a solve's stream time to its steps: an event is recorded at every phase change;
+// the time between consecutive events (device work plus any idle gap the host leaves) is charged
+// to the phase that was active.
+struct PhaseTimer {
+  static constexpr int kPhases = 12;
+  cudaStream_t s = nullptr;
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> ph;
+  double ms[kPhases] = {0};
+  int current = -1;
+
+  explicit PhaseTimer(cudaStream_t st) : s(st) {}
+  ~PhaseTimer() {
+    for (auto& e : ev) cudaEventDestroy(e);
+  }
+  PhaseTimer(const PhaseTimer&) = delete;
+  PhaseTimer& operator=(const PhaseTimer&) = delete;
+
+  void mark(int phase) {
+    if (ev.size() >= 8192) flush();
+    cudaEvent_t e;
+    TTGB_CUDA(cudaEventCreate(&e));
+    TTGB_CUDA(cudaEventRecord(e, s));
+    ev.push_back(e);
+    ph.push_back(phase);
+    current = phase;
+  }
+  void flush() {
+    if (ev.empty()) return;
+    TTGB_CUDA(cudaEventSynchronize(ev.back()));
+    for (size_t i = 0; i + 1 < ev.size(); ++i) {
+      float t = 0.f;
+      TTGB_CUDA(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
+      if (ph[i] >= 0 && ph[i] < kPhases) ms[ph[i]] += t;
+    }
+    cudaEvent_t last = ev.back();
+    const int lastph = ph.back();
+    for (size_t i = 0; i + 1 < ev.size(); ++i) cudaEventDestroy(ev[i]);
+    ev.clear();
+    ph.clear();
+    ev.push_back(last);
+    ph.push_back(lastph);
+  }
+};
+
 }  // namespace ttgb

@@ -24,6 +24,8 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--index", type=int, default=0)
     ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--profile", action="store_true", help="print the stream time per sweep step")
     args = ap.parse_args()
     if args.workload == "laplace_d8_n16":
         wl = W.laplace_d8_n16(args.seed)
@@ -40,11 +42,16 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         x, st = solve_cores(A, b, x0, nswp=p.get("nswp", 22), eps=p["eps"], kickrank=p["kickrank"],
-                            seed=args.seed + i, verbose=args.verbose)
+                            seed=args.seed + i, verbose=args.verbose, precision=args.precision,
+                            profile=args.profile)
         dt = time.perf_counter() - t0
         relres = float((TT(A) @ TT(x) - TT(b)).norm() / TT(b).norm())
+        if args.profile:
+            print(json.dumps({"phase_ms": {k: round(v, 2) for k, v in st["phase_ms"].items()},
+                              "host_syncs": st["host_syncs"]}), flush=True)
         print(json.dumps({"solve": i, "seconds": dt, "relres": relres, "sweeps": st["sweeps"],
                           "ranks": st["ranks"], "matvecs": st["matvecs"],
+                          "lowp_matvecs": st["lowp_matvecs"], "refinements": st["refinements"],
                           "gmres_iterations": st["gmres_iterations"]}), flush=True)
 
 

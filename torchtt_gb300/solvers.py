@@ -50,7 +50,7 @@ def _prep(cores, device):
 
 def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-10, rmax=32768,
                 max_full=500, kickrank=4, kick2=0, local_iterations=40, resets=2, verbose=False,
-                preconditioner=0, seed=1, stream=None):
+                preconditioner=0, seed=1, stream=None, precision="fp64", profile=False):
     """Native solve on lists of CUDA float64 cores; returns ``(x_cores, stats_dict)``.
 
     This is the thin layer over ``ttgb_amen_solve`` (include/ttgb300.h); ``amen_solve`` below adds
@@ -68,6 +68,10 @@ def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-
     p.kickrank, p.kick2 = int(kickrank), int(kick2)
     p.local_iterations, p.resets = int(local_iterations), int(resets)
     p.verbose, p.preconditioner, p.seed = int(bool(verbose)), int(preconditioner), int(seed)
+    if precision not in _lib.PRECISION:
+        raise InvalidArguments("precision must be 'fp64' or 'mixed'")
+    p.precision = _lib.PRECISION[precision]
+    p.profile = int(bool(profile))
     if stream is None:
         stream = torch.cuda.current_stream(A_cores[0].device)
     handle = _lib.c_vp()
@@ -101,7 +105,7 @@ def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-
 def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
                trunc_norm='res', local_solver=1, local_iterations=40, resets=2, verbose=False,
                preconditioner=None, use_cpp=True, band_diagonal=-1, use_single_precision=False,
-               backend='gb300', seed=1, z0=None, return_stats=False):
+               backend='gb300', seed=1, z0=None, return_stats=False, precision=None):
     """Solve the multilinear system A x = b in the TT format with AMEn on the GPU.
 
     Arguments are those of ``torchtt.solvers.amen_solve`` (``torchtt/solvers.py:211``), with the same
@@ -111,7 +115,10 @@ def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kick
     * ``seed``: seed of the counter-based RNG that draws the initial enrichment cores;
     * ``z0``: optional list of initial enrichment cores of ranks ``[1, kickrank+kick2, ..., 1]``
       (replays a given random start exactly);
-    * ``return_stats``: also return a dict of solver statistics.
+    * ``return_stats``: also return a dict of solver statistics;
+    * ``precision``: ``'fp64'`` (the reference's arithmetic) or ``'mixed'`` (low-precision local
+      GMRES operator inside FP64 iterative refinement). ``use_single_precision=True``, the
+      reference's own mixed mode (``torchtt/solvers.py:469-496``), selects ``'mixed'``.
     """
     # argument checks of torchtt/solvers.py:259-266
     if not (_is_tt(A) and _is_tt(b)):
@@ -138,7 +145,8 @@ def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kick
     cores, stats = solve_cores(Ac, bc, xc, zc, nswp=nswp, eps=eps, rmax=rmax, max_full=max_full,
                                kickrank=kickrank, kick2=kick2, local_iterations=local_iterations,
                                resets=resets, verbose=verbose, preconditioner=_PREC[preconditioner],
-                               seed=seed)
+                               seed=seed,
+                               precision=precision or ("mixed" if use_single_precision else "fp64"))
     cores = [c.to(device=out_device, dtype=out_dtype) for c in cores]
     cls = type(b) if _is_tt(b) else TT
     try:
