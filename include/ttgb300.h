@@ -64,6 +64,8 @@ typedef struct ttgb_amen_params {
   uint64_t seed;
   int32_t profile;              /* 1: time the contraction launches with CUDA events (stats) */
   int32_t precision;            /* TTGB_PRECISION_FP64 (default) or TTGB_PRECISION_MIXED */
+  int32_t lowp_engine;          /* MIXED only: 0 auto (TTGB_ENGINE_TC when available),
+                                   TTGB_ENGINE_FP32 or TTGB_ENGINE_TC */
 } ttgb_amen_params;
 
 /* Precision modes. FP64: the reference's arithmetic. MIXED: the local GMRES applies the projected
@@ -95,6 +97,8 @@ typedef struct ttgb_stats {
   double phase_ms[12];          /* profile only: stream time per sweep step - backward z, backward
                                    QR, backward interfaces, forward setup, local solve, SVD, rank
                                    search, forward z, enrichment, forward interfaces, other */
+  double lowp_ms;               /* profile + mixed: device time of the low-precision products */
+  int64_t lowp_launches;        /* profile + mixed: kernel launches of those products */
 } ttgb_stats;
 
 typedef struct ttgb_solution ttgb_solution;   /* opaque, library-owned result */
@@ -120,6 +124,29 @@ int ttgb_solution_copy_core(const ttgb_solution* sol, int32_t k, double* dst, in
                             void* stream);
 void ttgb_solution_free(ttgb_solution* sol);
 
+/* ---- batched / served solves ------------------------------------------------------------------
+ * A server runs up to `slots` solves at once on the current device, each on its own stream and
+ * host thread, so their kernels overlap on the GPU (continuous batching: a request is admitted as
+ * soon as a slot is free and its estimated HBM footprint - cores, interfaces and Krylov basis at an
+ * estimated final rank - fits in `mem_budget_bytes`; 0 means 80% of the free device memory).
+ * Requests are FIFO. The input cores of a request must stay valid until it completes. A request's
+ * result does not depend on what else is in flight (per-request RNG seed, per-request stream). */
+typedef struct ttgb_server ttgb_server;
+int ttgb_server_create(int32_t slots, int64_t mem_budget_bytes, ttgb_server** out);
+/* Queues A x = b (same arguments as ttgb_amen_solve without z0/stream); *id identifies it. */
+int ttgb_server_submit(ttgb_server* srv, const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0,
+                       const ttgb_amen_params* params, int64_t* id);
+/* Waits up to timeout_s (< 0: forever) for request id. On completion returns the request's status
+ * (TTGB_OK and *out = its solution, owned by the caller; or the error of the solve) and its times:
+ * queue_ms (submit to start) and run_ms (start to end). Returns TTGB_ERR_TIMEOUT if still running. */
+int ttgb_server_wait(ttgb_server* srv, int64_t id, double timeout_s, ttgb_solution** out,
+                     double* queue_ms, double* run_ms);
+/* Server counters: requests submitted, completed, running now, peak concurrently running. */
+int ttgb_server_stats(const ttgb_server* srv, int64_t* submitted, int64_t* completed,
+                      int32_t* running, int32_t* peak_running);
+/* Finishes queued and running requests, then frees the server. */
+void ttgb_server_destroy(ttgb_server* srv);
+
 /* ---- kernel-level entry points (FP64, device pointers, workspace allocated internally) ---- */
 
 /* y[l,m,L] = sum Phi_l[l,s,r] A[s,m,n,S] Phi_r[L,S,R] x[r,n,R]
@@ -128,6 +155,18 @@ void ttgb_solution_free(ttgb_solution* sol);
 int ttgb_local_product(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, int64_t S,
                        int64_t RL, int64_t R, const double* phi_l, const double* A,
                        const double* phi_r, const double* x, double* y, int32_t nrhs, void* stream);
+
+/* The local product with a low-precision engine (the operator of the mixed path's inner GMRES):
+ * FP64 in and out, contraction in TTGB_ENGINE_FP32 (CUDA-core FFMA) or TTGB_ENGINE_TC
+ * (tcgen05 tensor cores, 3xTF32 with FP32 accumulation in tensor memory). Same shapes as
+ * ttgb_local_product with one right-hand side. No counterpart in the reference (its only mixed mode
+ * is the FP32 GMRES of torchtt/solvers.py:469-496). */
+#define TTGB_ENGINE_FP32 1
+#define TTGB_ENGINE_TC 2
+int ttgb_local_product_lowp(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, int64_t S,
+                            int64_t RL, int64_t R, const double* phi_l, const double* A,
+                            const double* phi_r, const double* x, double* y, int32_t engine,
+                            void* stream);
 
 /* The same product as ttgb_local_product for callers that must not allocate device memory while
  * they run (a serving loop that reserved its HBM up front and admits work by footprint, code inside
@@ -180,6 +219,10 @@ int ttgb_local_gmres(int64_t r, int64_t s, int64_t n, int64_t S, int64_t R, cons
 
 /* Number of kernels this library has launched in the process so far. */
 int64_t ttgb_launch_count(void);
+
+/* Measured peak of this GPU's FMA pipe in TFLOP/s (dtype 0: FP64, 1: FP32): independent FMA
+   chains on every SM, best of three timed launches (about 50 ms each). */
+int ttgb_calibrate_fma(int32_t dtype, double* tflops);
 
 /* Message of the last error on this thread. */
 const char* ttgb_last_error(void);

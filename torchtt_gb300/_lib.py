@@ -30,7 +30,7 @@ class AmenParams(ctypes.Structure):
     _fields_ = [("nswp", c_i32), ("eps", c_dbl), ("rmax", c_i64), ("max_full", c_i64),
                 ("kickrank", c_i32), ("kick2", c_i32), ("local_iterations", c_i32),
                 ("resets", c_i32), ("verbose", c_i32), ("preconditioner", c_i32), ("seed", c_u64),
-                ("profile", c_i32), ("precision", c_i32)]
+                ("profile", c_i32), ("precision", c_i32), ("lowp_engine", c_i32)]
 
 PRECISION = {"fp64": 0, "mixed": 1}
 
@@ -42,7 +42,7 @@ class Stats(ctypes.Structure):
                 ("other_flops", c_dbl), ("host_syncs", c_i64), ("contract_ms", c_dbl),
                 ("contract_launches", c_i64), ("contract_flops", c_dbl),
                 ("lowp_matvecs", c_i64), ("lowp_flops", c_dbl), ("refinements", c_i64),
-                ("phase_ms", c_dbl * 12)]
+                ("phase_ms", c_dbl * 12), ("lowp_ms", c_dbl), ("lowp_launches", c_i64)]
 
     PHASES = ("bwd_z", "bwd_qr", "bwd_phi", "fwd_setup", "local_solve", "svd", "rank_search",
               "fwd_z", "enrichment", "fwd_phi", "other")
@@ -66,6 +66,7 @@ _SIGS = {
     "ttgb_solution_free": (None, [c_vp]),
     "ttgb_local_product": (c_i32, [c_i64] * 8 + [c_vp] * 5 + [c_i32, c_vp]),
     "ttgb_local_product_noalloc": (c_i32, [c_i64] * 8 + [c_vp] * 5 + [c_i32, c_vp]),
+    "ttgb_local_product_lowp": (c_i32, [c_i64] * 8 + [c_vp] * 5 + [c_i32, c_vp]),
     "ttgb_phi_fwd_A": (c_i32, [c_i64] * 8 + [c_vp] * 5 + [c_vp]),
     "ttgb_phi_bck_A": (c_i32, [c_i64] * 8 + [c_vp] * 5 + [c_vp]),
     "ttgb_phi_fwd_rhs": (c_i32, [c_i64] * 5 + [c_vp] * 4 + [c_vp]),
@@ -74,7 +75,17 @@ _SIGS = {
     "ttgb_svd": (c_i32, [c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp]),
     "ttgb_local_gmres": (c_i32, [c_i64] * 5 + [c_vp] * 5 + [c_i32, c_dbl, c_i32, c_i32,
                                                           ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_vp]),
+    "ttgb_server_create": (c_i32, [c_i32, c_i64, ctypes.POINTER(c_vp)]),
+    "ttgb_server_submit": (c_i32, [c_vp, ctypes.POINTER(TTDesc), ctypes.POINTER(TTDesc),
+                                   ctypes.POINTER(TTDesc), ctypes.POINTER(AmenParams),
+                                   ctypes.POINTER(c_i64)]),
+    "ttgb_server_wait": (c_i32, [c_vp, c_i64, c_dbl, ctypes.POINTER(c_vp), ctypes.POINTER(c_dbl),
+                                 ctypes.POINTER(c_dbl)]),
+    "ttgb_server_stats": (c_i32, [c_vp, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64),
+                                  ctypes.POINTER(c_i32), ctypes.POINTER(c_i32)]),
+    "ttgb_server_destroy": (None, [c_vp]),
     "ttgb_launch_count": (c_i64, []),
+    "ttgb_calibrate_fma": (c_i32, [c_i32, ctypes.POINTER(c_dbl)]),
     "ttgb_last_error": (ctypes.c_char_p, []),
     "ttgb_version": (c_i32, []),
 }

@@ -117,6 +117,7 @@ class AmenRun {
     dscal_.reset(kScal, s_);
     if (p.profile) {
       prof_.reset(new Profiler(s_));
+      prof_lowp_.reset(new Profiler(s_));
       phases_.reset(new PhaseTimer(s_));
     }
   }
@@ -125,6 +126,7 @@ class AmenRun {
     if (red_counter_) cudaFreeAsync(red_counter_, s_);
     if (lws_.status) cudaFreeAsync(lws_.status, s_);
     if (gws_.d_flag) cudaFreeAsync(gws_.d_flag, s_);
+    if (tc_err_) cudaFreeAsync(tc_err_, s_);
     if (hbuf_) cudaFreeHost(hbuf_);
   }
 
@@ -155,11 +157,16 @@ class AmenRun {
   DBuf w1_, w2_, wp_, wphi_, wrhs_, prec_J_, prec_work_;
   AmenStats st_;
   std::unique_ptr<Profiler> prof_;
+  std::unique_ptr<Profiler> prof_lowp_;
   int64_t op_count_ = 0;   // applications of the current local operator
   int64_t lowp_count_ = 0; // low-precision applications of the current local operator
   bool mixed_ = false;
-  std::vector<FBuf> A32_;  // FP32 copies of the A cores (mixed path)
+  std::vector<FBuf> A32_;  // FP32 copies of the A cores (mixed path, FP32 engine)
   FBuf phil32_, phir32_, xf_, yf_, w1f_, w2f_;
+  bool use_tc_ = false;    // mixed path on the tcgen05 engine
+  std::vector<TcCore> tc_cores_;
+  TcLocal tc_local_;
+  int* tc_err_ = nullptr;
   DBuf resvec_;
   uint64_t rng_offset_ = 0;
 
@@ -278,11 +285,20 @@ void AmenRun::init(const TTView& x0, const TTView& z0) {
   const int d = d_;
   mixed_ = p_.precision == 1;
   if (mixed_) {
-    A32_.resize(d);
-    for (int i = 0; i < d; ++i) {
-      const int64_t ne = rA_[i] * N_[i] * N_[i] * rA_[i + 1];
-      A32_[i].reset((size_t)ne, s_);
-      cast(Acore(i), A32_[i].p, ne, s_);
+    use_tc_ = (p_.lowp_engine == 2) || (p_.lowp_engine == 0 && tc_available());
+    TTGB_REQUIRE(!use_tc_ || tc_available(), "tcgen05 engine needs an sm_100-family GPU");
+    if (use_tc_) {
+      tc_cores_.resize(d);
+      for (int i = 0; i < d; ++i) tc_cores_[i].build(Acore(i), rA_[i], N_[i], N_[i], rA_[i + 1], s_);
+      TTGB_CUDA(cudaMallocAsync((void**)&tc_err_, sizeof(int), s_));
+      TTGB_CUDA(cudaMemsetAsync(tc_err_, 0, sizeof(int), s_));
+    } else {
+      A32_.resize(d);
+      for (int i = 0; i < d; ++i) {
+        const int64_t ne = rA_[i] * N_[i] * N_[i] * rA_[i + 1];
+        A32_[i].reset((size_t)ne, s_);
+        cast(Acore(i), A32_[i].p, ne, s_);
+      }
     }
   }
   x_.resize(d);
@@ -704,6 +720,16 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
 // FP32 copies of the local operator for the low-precision engine (mixed path)
 void AmenRun::setup_lowp(LocalOperator& op, int k) {
   const LocalOpDims& d = op.dims;
+  if (use_tc_) {
+    tc_local_.setup(d, Phis_[k].data(), Phis_[k + 1].data(), &tc_cores_[k], tc_err_, s_);
+    op.lowp = true;
+    op.tc = &tc_local_;
+    lowp_count_ = 0;
+    op.count_lowp = &lowp_count_;
+  op.prof_lowp = prof_lowp_.get();
+    op.prof_lowp = prof_lowp_.get();
+    return;
+  }
   phil32_.ensure((size_t)(d.rl * d.s * d.r), s_);
   phir32_.ensure((size_t)(d.RL * d.S * d.R), s_);
   cast(Phis_[k].data(), phil32_.p, d.rl * d.s * d.r, s_);
@@ -723,6 +749,7 @@ void AmenRun::setup_lowp(LocalOperator& op, int k) {
   op.w2f = w2f_.p;
   lowp_count_ = 0;
   op.count_lowp = &lowp_count_;
+  op.prof_lowp = prof_lowp_.get();
 }
 
 // Mixed-path rank search (same rule as amen_solve.h:385-403): the candidate of rank rr leaves out
@@ -823,6 +850,11 @@ AmenResult AmenRun::run(const TTView& x0, const TTView& z0) {
   }
   res.ranks = rx_;
   TTGB_CUDA(cudaStreamSynchronize(s_));
+  if (tc_err_) {
+    int herr = 0;
+    TTGB_CUDA(cudaMemcpy(&herr, tc_err_, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) throw Error(kTimeout, "tcgen05 GEMM: a bounded wait gave up");
+  }
   if (phases_) {
     phases_->flush();
     for (int i = 0; i < PhaseTimer::kPhases && i < 12; ++i) st_.phase_ms[i] = phases_->ms[i];
@@ -832,6 +864,9 @@ AmenResult AmenRun::run(const TTView& x0, const TTView& z0) {
     st_.contract_ms = prof_->ms;
     st_.contract_launches = prof_->launches;
     st_.contract_flops = prof_->flops;
+    prof_lowp_->flush();
+    st_.lowp_ms = prof_lowp_->ms;
+    st_.lowp_launches = prof_lowp_->launches;
   }
   res.stats = st_;
   return res;

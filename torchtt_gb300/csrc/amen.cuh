@@ -26,6 +26,7 @@ struct AmenParams {
   // evaluates candidates as res - B tail (FP64 residual, low-precision product of the small tail).
   int precision = 0;
   int max_refine = 4;          // refinement steps per local solve (mixed)
+  int lowp_engine = 0;         // mixed: 0 auto (tcgen05 when available), 1 FP32 CUDA cores, 2 tcgen05
   double lowp_floor = 1e-5;    // relative target of one low-precision inner solve (mixed)
 };
 
@@ -57,6 +58,9 @@ struct AmenStats {
   // interfaces, forward setup, local solve, SVD, rank search, forward z, enrichment, forward
   // interfaces, other
   double phase_ms[12] = {0};
+  // profile only: CUDA-event time of the low-precision local products (mixed path)
+  double lowp_ms = 0.0;
+  int64_t lowp_launches = 0;
   // filled when AmenParams::profile is set: CUDA-event time of the contraction launches
   double contract_ms = 0.0;
   int64_t contract_launches = 0;

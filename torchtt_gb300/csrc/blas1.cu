@@ -1,5 +1,7 @@
 // Vector kernels: two-stage deterministic reductions and element-wise updates (FP64).
 #include <atomic>
+#include <map>
+#include <mutex>
 
 #include "blas1.cuh"
 
@@ -8,6 +10,18 @@ namespace ttgb {
 static std::atomic<int64_t> g_launches{0};
 int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+void smem_optin(const void* kernel, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> done;
+  int dev = 0;
+  TTGB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  int& cur = done[std::make_pair(kernel, dev)];
+  if (cur >= bytes) return;
+  TTGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  cur = bytes;
+}
 
 namespace {
 

@@ -5,17 +5,17 @@
 
 #include "../../include/ttgb300.h"
 #include "amen.cuh"
+#include "solution.cuh"
 #include "blas1.cuh"
 #include "contract.cuh"
 #include "gmres.cuh"
 #include "linalg.cuh"
 #include "prec.cuh"
+#include "tc_gemm.cuh"
+#include "tc_local.cuh"
 
 using namespace ttgb;
 
-struct ttgb_solution {
-  AmenResult res;
-};
 
 namespace {
 
@@ -122,6 +122,7 @@ void ttgb_default_params(ttgb_amen_params* p) {
   p->seed = 1;
   p->profile = 0;
   p->precision = TTGB_PRECISION_FP64;
+  p->lowp_engine = 0;
 }
 
 int ttgb_amen_solve(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, const ttgb_tt* z0,
@@ -146,6 +147,8 @@ int ttgb_amen_solve(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, const
     TTGB_REQUIRE(params->precision == TTGB_PRECISION_FP64 || params->precision == TTGB_PRECISION_MIXED,
                  "invalid precision mode");
     p.precision = params->precision;
+    TTGB_REQUIRE(params->lowp_engine >= 0 && params->lowp_engine <= 2, "invalid low-precision engine");
+    p.lowp_engine = params->lowp_engine;
     auto* sol = new ttgb_solution;
     try {
       sol->res = amen_solve(Av, bv, xv, zv, p, as_stream(stream));
@@ -188,6 +191,8 @@ int ttgb_solution_stats(const ttgb_solution* sol, ttgb_stats* st) {
     st->lowp_flops = a.lowp_flops;
     st->refinements = a.refinements;
     for (int i = 0; i < 12; ++i) st->phase_ms[i] = a.phase_ms[i];
+    st->lowp_ms = a.lowp_ms;
+    st->lowp_launches = a.lowp_launches;
   });
 }
 
@@ -224,6 +229,48 @@ int ttgb_local_product(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, i
     for (int32_t i = 0; i < nrhs; ++i)
       local_product(d, phi_l, A, phi_r, x + (int64_t)i * r * n * R, y + (int64_t)i * rl * m * RL,
                     w1.p, w2.p, st);
+  });
+}
+
+int ttgb_local_product_lowp(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, int64_t S,
+                            int64_t RL, int64_t R, const double* phi_l, const double* A,
+                            const double* phi_r, const double* x, double* y, int32_t engine,
+                            void* stream) {
+  return guarded([&] {
+    TTGB_REQUIRE(rl > 0 && s > 0 && r > 0 && m > 0 && n > 0 && S > 0 && RL > 0 && R > 0,
+                 "non-positive dimension");
+    TTGB_REQUIRE(phi_l && A && phi_r && x && y, "null pointer");
+    TTGB_REQUIRE(engine == TTGB_ENGINE_FP32 || engine == TTGB_ENGINE_TC, "unknown engine");
+    cudaStream_t st = as_stream(stream);
+    LocalOpDims d{rl, s, r, m, n, S, RL, R};
+    if (engine == TTGB_ENGINE_TC) {
+      TTGB_REQUIRE(tc_available(), "tcgen05 engine needs an sm_100-family GPU");
+      int* err = nullptr;
+      TTGB_CUDA(cudaMallocAsync((void**)&err, sizeof(int), st));
+      TTGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+      {
+        TcCore core;
+        core.build(A, s, m, n, S, st);
+        TcLocal tl;
+        tl.setup(d, phi_l, phi_r, &core, err, st);
+        tl.apply(x, y, st);
+        int herr = 0;
+        TTGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TTGB_CUDA(cudaStreamSynchronize(st));
+        cudaFreeAsync(err, st);
+        if (herr) throw Error(kTimeout, "tcgen05 GEMM: a bounded wait gave up");
+      }
+    } else {
+      const size_t nx = (size_t)(r * n * R), ny = (size_t)(rl * m * RL);
+      FBuf pl((size_t)(rl * s * r), st), a32((size_t)(s * m * n * S), st), pr((size_t)(RL * S * R), st);
+      FBuf xf(nx, st), yf(ny, st), w1(local_product_w1(d), st), w2(local_product_w2(d), st);
+      cast(phi_l, pl.p, rl * s * r, st);
+      cast(A, a32.p, s * m * n * S, st);
+      cast(phi_r, pr.p, RL * S * R, st);
+      cast(x, xf.p, (int64_t)nx, st);
+      local_product(d, pl.p, a32.p, pr.p, xf.p, yf.p, w1.p, w2.p, st);
+      cast(yf.p, y, (int64_t)ny, st);
+    }
   });
 }
 
@@ -349,6 +396,13 @@ int ttgb_local_gmres(int64_t r, int64_t s, int64_t n, int64_t S, int64_t R, cons
 const char* ttgb_last_error(void) { return g_last_error.c_str(); }
 
 int64_t ttgb_launch_count(void) { return launch_count(); }
+
+int ttgb_calibrate_fma(int32_t dtype, double* tflops) {
+  return guarded([&] {
+    TTGB_REQUIRE(tflops != nullptr && (dtype == 0 || dtype == 1), "invalid calibration request");
+    *tflops = calibrate_fma(dtype);
+  });
+}
 
 int32_t ttgb_version(void) { return 100; }
 

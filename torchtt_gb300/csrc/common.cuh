@@ -45,6 +45,8 @@ struct Error : std::runtime_error {
 
 // Every kernel launch of the library is followed by TTGB_CHECK_LAUNCH(), which also counts it.
 int64_t launch_count();
+// measured FMA-pipe peak in TFLOP/s (0: FP64, 1: FP32), see calibrate.cu
+double calibrate_fma(int dtype);
 void count_launch();
 #define TTGB_CHECK_LAUNCH()                 \
   do {                                      \
@@ -69,6 +71,10 @@ inline int num_sms() {
 }
 
 inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+
+// Raises a kernel's dynamic shared-memory limit to `bytes` on the current device, calling the
+// runtime only when the cached limit for that (kernel, device) is lower.
+void smem_optin(const void* kernel, int bytes);
 
 // A stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync from the device's default
 // memory pool, whose release threshold the solver raises so that freed blocks are reused).

@@ -14,9 +14,15 @@ void LocalOperator::apply(const double* x, double* y, bool use_prec, cudaStream_
     in = wp;
   }
   if (lowp) {
-    cast(in, xf, size(), s);
-    local_product(dims, phi_l32, A32, phi_r32, xf, yf, w1f, w2f, s);
-    cast(yf, y, dims.rl * dims.m * dims.RL, s);
+    if (prof_lowp) prof_lowp->begin();
+    if (tc) {
+      tc->apply(in, y, s);
+    } else {
+      cast(in, xf, size(), s);
+      local_product(dims, phi_l32, A32, phi_r32, xf, yf, w1f, w2f, s);
+      cast(yf, y, dims.rl * dims.m * dims.RL, s);
+    }
+    if (prof_lowp) prof_lowp->end(local_product_flops(dims), tc ? 4 : 5);
     if (count_lowp) ++*count_lowp;
     return;
   }

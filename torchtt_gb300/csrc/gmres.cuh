@@ -5,6 +5,7 @@
 #include "blas1.cuh"
 #include "contract.cuh"
 #include "profiler.cuh"
+#include "tc_local.cuh"
 
 namespace ttgb {
 
@@ -41,6 +42,8 @@ struct LocalOperator {
   float* yf = nullptr;          // N_loc
   float* w1f = nullptr;
   float* w2f = nullptr;
+  TcLocal* tc = nullptr;        // when set, the low-precision engine is the tcgen05 3xTF32 GEMM
+  Profiler* prof_lowp = nullptr;  // optional timing of the low-precision products
   int64_t* count_lowp = nullptr;
   int64_t size() const { return dims.r * dims.n * dims.R; }
   void apply(const double* x, double* y, bool use_prec, cudaStream_t s) const;

@@ -699,8 +699,8 @@ QRResult qr(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, doubl
     gemm_cm(Ain, ldin, Ain, ldin, G, n, n, n, m, 1.0, 0.0, s, true, false);
     if (n <= kCholSmemMax) {
       const size_t smem = (size_t)2 * n * (n + 1) * sizeof(double);
-      TTGB_CUDA(cudaFuncSetAttribute(chol_inv_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(2 * kCholSmemMax * (kCholSmemMax + 1) * sizeof(double))));
+      smem_optin((const void*)chol_inv_smem_kernel,
+                 (int)(2 * kCholSmemMax * (kCholSmemMax + 1) * sizeof(double)));
       chol_inv_smem_kernel<<<1, 512, smem, s>>>(G, (int)n, pass == 0 ? m : 0, pass == 2 ? 1 : 0, G,
                                                 Ri, ws.status);
       TTGB_CHECK_LAUNCH();
@@ -761,8 +761,7 @@ void svd(const double* A, int64_t lda, int64_t m, int64_t n, double* U, double* 
   if (n <= kJacobiClusterMaxN && n >= 2 * kJacobiCluster) {
     const int ncl = (int)((n + kJacobiCluster - 1) / kJacobiCluster);
     const size_t smem = (size_t)2 * ncl * n * sizeof(double);
-    TTGB_CUDA(cudaFuncSetAttribute(jacobi_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
+    smem_optin((const void*)jacobi_cluster_kernel, (int)smem);
     jacobi_cluster_kernel<<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status);
     TTGB_CHECK_LAUNCH();
     DBuf sig((size_t)n, s);
@@ -774,10 +773,7 @@ void svd(const double* A, int64_t lda, int64_t m, int64_t n, double* U, double* 
   }
   const size_t smem = (size_t)2 * n * n * sizeof(double);
   const int use_smem = smem <= 200 * 1024 ? 1 : 0;
-  if (use_smem) {
-    TTGB_CUDA(cudaFuncSetAttribute(jacobi_svd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-  }
+  if (use_smem) smem_optin((const void*)jacobi_svd_kernel, (int)smem);
   jacobi_svd_kernel<<<1, 512, use_smem ? smem : 0, s>>>(W, Vw, (int)n, Up.p, S, use_smem, 60,
                                                          ws.status, nullptr);
   TTGB_CHECK_LAUNCH();

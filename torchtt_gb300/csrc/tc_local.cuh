@@ -1,0 +1,31 @@
+// The local AMEn product on the tcgen05 engine (3xTF32, FP32 accumulation in tensor memory):
+// y[l,m,L] = sum Phi_l[l,s,r] A[s,m,n,S] Phi_r[L,S,R] x[r,n,R] as three tensor-core GEMMs whose
+// operands are all K-major:
+//   W [l][R][s][n]  = x^P [(n,R), r]   . Phi_l [(l,s), r]^T       (x^P: x gathered to (n,R,r))
+//   Y2[l][m][S][R]  = A'  [(m,S),(s,n)] . W_l  [R, (s,n)]^T        (batched over l; A' = A permuted)
+//   y [l][m][L]     = Y2  [(l,m),(S,R)] . Phi_r [L, (S,R)]^T
+// Each epilogue writes the next operand directly as a TF32 hi/lo split; the last writes FP64.
+#pragma once
+
+#include "contract.cuh"
+#include "tc_gemm.cuh"
+
+namespace ttgb {
+
+// A' [(m,S),(s,n)] split of one A core (s x m x n x S), shared by every local problem of that core
+struct TcCore {
+  FBuf hi, lo;
+  void build(const double* A, int64_t s, int64_t m, int64_t n, int64_t S, cudaStream_t st);
+};
+
+struct TcLocal {
+  LocalOpDims d{};
+  const TcCore* core = nullptr;
+  FBuf phl_h, phl_l, phr_h, phr_l, xh, xl, wh, wl, yh, yl;
+  int* err = nullptr;   // device flag of the bounded waits
+  void setup(const LocalOpDims& dims, const double* phi_l, const double* phi_r, const TcCore* c,
+             int* errflag, cudaStream_t st);
+  void apply(const double* x, double* y, cudaStream_t st);
+};
+
+}  // namespace ttgb

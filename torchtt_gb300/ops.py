@@ -125,3 +125,21 @@ def local_gmres(Phi_left, coreA, Phi_right, rhs, iters=40, threshold=1e-10, rese
                                            int(prec), ctypes.byref(flag), ctypes.byref(nit),
                                            _stream(rhs.device)))
     return x, flag.value, nit.value
+
+
+ENGINE_FP32 = 1
+ENGINE_TC = 2
+
+
+def local_product_lowp(Phi_right, Phi_left, coreA, core, engine=ENGINE_TC):
+    """The local product with a low-precision engine (FP32 CUDA cores or tcgen05 3xTF32),
+    FP64 in and out: the operator of the mixed path's inner GMRES."""
+    _dev64(Phi_right, Phi_left, coreA, core)
+    rl, s, r = Phi_left.shape
+    _, m, n, S = coreA.shape
+    RL, _, R = Phi_right.shape
+    y = torch.empty((rl, m, RL), dtype=torch.float64, device=core.device)
+    _lib.check(_lib.lib().ttgb_local_product_lowp(rl, s, r, m, n, S, RL, R, _ptr(Phi_left), _ptr(coreA),
+                                                  _ptr(Phi_right), _ptr(core), _ptr(y), int(engine),
+                                                  _stream(core.device)))
+    return y

@@ -26,6 +26,8 @@ def main():
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--profile", action="store_true", help="print the stream time per sweep step")
+    ap.add_argument("--engine", default="auto", choices=["auto", "fp32", "tc"],
+                    help="low-precision engine of the mixed path")
     args = ap.parse_args()
     if args.workload == "laplace_d8_n16":
         wl = W.laplace_d8_n16(args.seed)
@@ -43,7 +45,7 @@ def main():
         t0 = time.perf_counter()
         x, st = solve_cores(A, b, x0, nswp=p.get("nswp", 22), eps=p["eps"], kickrank=p["kickrank"],
                             seed=args.seed + i, verbose=args.verbose, precision=args.precision,
-                            profile=args.profile)
+                            profile=args.profile, engine=args.engine)
         dt = time.perf_counter() - t0
         relres = float((TT(A) @ TT(x) - TT(b)).norm() / TT(b).norm())
         if args.profile:

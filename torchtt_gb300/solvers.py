@@ -50,7 +50,8 @@ def _prep(cores, device):
 
 def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-10, rmax=32768,
                 max_full=500, kickrank=4, kick2=0, local_iterations=40, resets=2, verbose=False,
-                preconditioner=0, seed=1, stream=None, precision="fp64", profile=False):
+                preconditioner=0, seed=1, stream=None, precision="fp64", profile=False,
+                engine="auto"):
     """Native solve on lists of CUDA float64 cores; returns ``(x_cores, stats_dict)``.
 
     This is the thin layer over ``ttgb_amen_solve`` (include/ttgb300.h); ``amen_solve`` below adds
@@ -72,6 +73,10 @@ def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-
         raise InvalidArguments("precision must be 'fp64' or 'mixed'")
     p.precision = _lib.PRECISION[precision]
     p.profile = int(bool(profile))
+    engines = {"auto": 0, "fp32": 1, "tc": 2}
+    if engine not in engines:
+        raise InvalidArguments("engine must be 'auto', 'fp32' or 'tc'")
+    p.lowp_engine = engines[engine]
     if stream is None:
         stream = torch.cuda.current_stream(A_cores[0].device)
     handle = _lib.c_vp()
@@ -80,17 +85,23 @@ def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-
                                  ctypes.byref(dz) if dz is not None else None,
                                  ctypes.byref(p), ctypes.c_void_p(stream.cuda_stream),
                                  ctypes.byref(handle)))
+    return fetch_solution(handle, [int(c.shape[2]) for c in A_cores], A_cores[0].device, stream)
+
+
+def fetch_solution(handle, modes, device, stream):
+    """Copies the cores of a library-owned solution into new CUDA tensors, frees the handle and
+    returns ``(cores, stats)``."""
+    L = _lib.lib()
     try:
-        d = len(A_cores)
+        d = len(modes)
         dd = _lib.c_i32()
         ranks = (_lib.c_i64 * (d + 1))()
         _lib.check(L.ttgb_solution_dims(handle, ctypes.byref(dd), ranks))
         st = _lib.Stats()
         _lib.check(L.ttgb_solution_stats(handle, ctypes.byref(st)))
-        dev = A_cores[0].device
         out = []
         for k in range(d):
-            t = torch.empty((ranks[k], A_cores[k].shape[2], ranks[k + 1]), dtype=torch.float64, device=dev)
+            t = torch.empty((ranks[k], modes[k], ranks[k + 1]), dtype=torch.float64, device=device)
             _lib.check(L.ttgb_solution_copy_core(handle, k, ctypes.c_void_p(t.data_ptr()), 0,
                                                  ctypes.c_void_p(stream.cuda_stream)))
             out.append(t)
@@ -100,6 +111,27 @@ def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-
     stats = st.as_dict()
     stats["ranks"] = [int(r) for r in ranks]
     return out, stats
+
+
+def make_params(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
+                local_iterations=40, resets=2, verbose=False, preconditioner=0, seed=1,
+                precision="fp64", profile=False, engine="auto"):
+    """A ``ttgb_amen_params`` structure from keyword arguments (defaults of the reference)."""
+    p = _lib.AmenParams()
+    _lib.lib().ttgb_default_params(ctypes.byref(p))
+    p.nswp, p.eps, p.rmax, p.max_full = int(nswp), float(eps), int(rmax), int(max_full)
+    p.kickrank, p.kick2 = int(kickrank), int(kick2)
+    p.local_iterations, p.resets = int(local_iterations), int(resets)
+    p.verbose, p.preconditioner, p.seed = int(bool(verbose)), int(preconditioner), int(seed)
+    if precision not in _lib.PRECISION:
+        raise InvalidArguments("precision must be 'fp64' or 'mixed'")
+    p.precision = _lib.PRECISION[precision]
+    p.profile = int(bool(profile))
+    engines = {"auto": 0, "fp32": 1, "tc": 2}
+    if engine not in engines:
+        raise InvalidArguments("engine must be 'auto', 'fp32' or 'tc'")
+    p.lowp_engine = engines[engine]
+    return p
 
 
 def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
