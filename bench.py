@@ -1,19 +1,27 @@
-"""Benchmark: AMEn solves/s (and per-solve latency) on one GB300.
+"""Benchmark: AMEn solves/s and per-request p50/p99 latency on one GB300, mixed precision, batched.
 
-Workload (default): the single large solve - d=20, n=64, A = Kronecker-sum Laplacian
-(n+1)^2 tridiag(-1,2,-1) plus the product potential (x)_k diag(1 + 0.5 cos(2 pi i/n)) (TT rank 3),
-b = random TT of rank 8 with N(0,1) cores (seeded, ||b|| = 1), x0 = ones, eps = 1e-8, kickrank 8,
-nswp 20. One step = one complete solve. Synthetic seeded data; no dataset is involved.
+Workload: the single large solve, d=20, n=64. A = Kronecker-sum Laplacian (n+1)^2 tridiag(-1,2,-1)
+plus the product potential (x)_k diag(1 + 0.5 cos(2 pi i/n)) (TT rank 3); b_j = random TT of rank
+8 with N(0,1) cores from seed (seed + j), ||b_j|| = 1; x0 = ones; eps 1e-8, kickrank 8, nswp 20.
+Synthetic seeded data; no dataset is involved.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--batch B]
 
-* gb300 arm: W warm-up solves, then K timed solves bracketed by barrier + synchronize (CUDA events
-  on the solve stream), an L2 flush (256 MiB write) between solves; ``value`` = total solves / s over
-  all ranks (weak scaling: every rank solves its own copy of the workload). ``e2e`` repeats the
-  solve through the public API (``torchtt_gb300.amen_solve``) with CPU-resident TT cores, so host to
-  device copies of A and b and the copy of x back are inside the timed region.
+* gb300 arm. One step = one batch of B (default 8) such solves (the same A, B right-hand sides)
+  submitted together to the request server (``torchtt_gb300.serving.Server`` with B slots): each
+  solve runs the mixed-precision path (low-precision local GMRES operator inside FP64 iterative
+  refinement) on its own stream and host thread, so the batch overlaps on the device. W untimed
+  warm-up steps, then K timed steps bracketed by barrier + synchronize, CUDA events on the
+  submitting stream around each step (the host waits for every result inside the step), a 256 MiB
+  L2 flush write between steps. ``value`` = solves / s over all ranks (weak scaling: every rank
+  serves its own batch). Beside it, measured in the same run: the plain FP64 path one solve at a
+  time (the baseline the mixed/batched path is compared with), the mixed path unbatched, the FP64
+  path batched, the relative residual of every solution and ||x_mixed - x_fp64|| / ||x_fp64||.
+  ``e2e`` repeats batched steps with host-resident (pinned) inputs through the public API, so the
+  host-to-device copies of A and every b_j and the copies of the solutions back are timed.
 * reference arm: the reference's CPU algorithm (the numpy restatement in oracle/, on all host
-  threads; the compiled reference cannot be built on the GPU host) on rank 0 only, same workload.
+  threads; the compiled reference is not available on the GPU host) on rank 0 only, one solve of
+  the same workload per step.
 """
 import argparse
 import json
@@ -28,7 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = ("laplace_potential_d20_n64", "laplace_d8_n16")
-FP64_PEAK_TFLOPS = 1.20   # measured FP64 FMA-pipe rate of this GB300 pool (profiles/fp64_fma_peak.md)
+METRIC = "AMEn solves/s & p99 latency at rel. residual 1e-8: mixed/batched vs FP64 plain"
 
 
 def get_workload(name, seed):
@@ -38,6 +46,14 @@ def get_workload(name, seed):
     if name == "laplace_d8_n16":
         return W.laplace_d8_n16(seed)
     raise SystemExit("unknown workload " + name)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 def dist_env():
@@ -85,7 +101,7 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm, smax, reasons = [], [], set()
+        sm, smax, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -94,6 +110,7 @@ class ClockSampler:
             try:
                 sm.append(float(parts[1]))
                 smax.append(float(parts[2]))
+                power.append(float(parts[3]))
             except ValueError:
                 continue
             for nm, v in zip(names, parts[5:9]):
@@ -101,6 +118,7 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
+                "power_w_median": statistics.median(power) if power else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
@@ -125,42 +143,49 @@ def cpu_solve_once(wl):
     return time.perf_counter() - t0, info
 
 
+def workload_config(args, wl):
+    p = wl["params"]
+    return {"workload": args.workload, "d": len(wl["A"]), "n": int(wl["A"][0].shape[1]),
+            "A_rank": int(wl["A"][0].shape[-1]), "b_rank": int(wl["b"][0].shape[-1]),
+            "eps": p["eps"], "kickrank": p["kickrank"], "nswp": p.get("nswp", 22)}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    wl = get_workload(args.workload, args.seed)
     cores = os.cpu_count() or 1
     times = []
     for i in range(args.warmup + args.steps):
+        wl = get_workload(args.workload, args.seed + i % args.batch)
         dt, info = cpu_solve_once(wl)
         if i >= args.warmup:
             times.append(dt)
     total = sum(times)
     value = len(times) / total
+    cfg = workload_config(args, get_workload(args.workload, args.seed))
+    cfg.update({"precision": "fp64", "batch": 1, "l2": "host run"})
     line = {
-        "metric": "AMEn solves/s (single large solve, FP64 CPU reference algorithm)",
-        "impl": "reference", "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1000 * total / len(times), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": args.workload, "eps": wl["params"]["eps"],
-                   "kickrank": wl["params"]["kickrank"], "nswp": wl["params"].get("nswp", 22)},
+        "metric": METRIC, "impl": "reference", "value": value, "unit": "solves/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)", "config": cfg,
         "latency_ms": {"p50": 1000 * percentile(times, 0.5), "p99": 1000 * percentile(times, 0.99)},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": "%d full solves of %s, numpy/OpenBLAS on all host threads"
-                                   % (len(times), args.workload)},
+                         "sample": "%d full solves of %s (one per step), numpy/OpenBLAS on all host "
+                                   "threads" % (len(times), args.workload)},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def read_traffic(kernel_profile):
-    path = os.path.join(ROOT, "profiles", kernel_profile)
+def read_profile_value(name, key):
+    """A ``key: value`` line of a committed ncu summary (per-launch DRAM traffic)."""
     try:
-        for ln in open(path):
-            if ln.startswith("traffic_bytes_per_launch:"):
+        for ln in open(os.path.join(ROOT, "profiles", name)):
+            if ln.startswith(key + ":"):
                 return float(ln.split(":", 1)[1].split()[0])
-    except OSError:
+    except (OSError, ValueError):
         pass
     return None
 
@@ -179,42 +204,35 @@ def run_gb300(args):
         B.build()
     if ws > 1:
         dist.barrier()
-    from torchtt_gb300 import TT, amen_solve, _lib
+    from torchtt_gb300 import TT, _lib, ops
+    from torchtt_gb300.serving import Server
     from torchtt_gb300.solvers import solve_cores
 
-    wl = get_workload(args.workload, args.seed)
-    p = wl["params"]
-    kw = dict(nswp=p.get("nswp", 22), eps=p["eps"], kickrank=p["kickrank"], seed=args.seed + rank)
-    A_d = [c.to(dev) for c in wl["A"]]
-    b_d = [c.to(dev) for c in wl["b"]]
-    x0_d = [c.to(dev) for c in wl["x0"]] if wl.get("x0") is not None else None
+    nb = args.batch
+    seeds = [args.seed + rank * nb + j for j in range(nb)]
+    wls = [get_workload(args.workload, s) for s in seeds]
+    p = wls[0]["params"]
+    kw = dict(nswp=p.get("nswp", 22), eps=p["eps"], kickrank=p["kickrank"])
+    A_d = TT([c.to(dev) for c in wls[0]["A"]])
+    bs_d = [TT([c.to(dev) for c in w["b"]]) for w in wls]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
+    engine = args.engine
 
-    def solve(profile=0):
-        return solve_cores(A_d, b_d, x0_d, **kw, stream=stream) if not profile else \
-            _solve_profiled()
+    srv = Server(slots=nb, device=dev)
 
-    def _solve_profiled():
-        import ctypes
-        L = _lib.lib()
-        from torchtt_gb300.solvers import _desc
-        keep = []
-        dA, db = _desc(A_d, True, keep), _desc(b_d, False, keep)
-        dx = _desc(x0_d, False, keep) if x0_d else None
-        prm = _lib.AmenParams()
-        L.ttgb_default_params(ctypes.byref(prm))
-        prm.nswp, prm.eps, prm.kickrank, prm.seed, prm.profile = kw["nswp"], kw["eps"], kw["kickrank"], kw["seed"], 1
-        h = _lib.c_vp()
-        _lib.check(L.ttgb_amen_solve(ctypes.byref(dA), ctypes.byref(db), ctypes.byref(dx) if dx else None, None,
-                                     ctypes.byref(prm), ctypes.c_void_p(stream.cuda_stream), ctypes.byref(h)))
-        st = _lib.Stats()
-        L.ttgb_solution_stats(h, ctypes.byref(st))
-        L.ttgb_solution_free(h)
-        return None, st.as_dict()
+    def batch(precision, A=A_d, rhs=bs_d):
+        ids = [srv.submit(A, b, precision=precision, engine=engine, seed=1000 + j, **kw)
+               for j, b in enumerate(rhs)]
+        return [srv.result(i) for i in ids]
 
+    def single(precision, j=0, profile=False):
+        return solve_cores(A_d.cores, bs_d[j].cores, precision=precision, engine=engine,
+                           seed=1000 + j, profile=profile, stream=stream, **kw)
+
+    # ---- headline: mixed precision, batched through the server --------------------------------
     for _ in range(args.warmup):
-        solve()
+        batch("mixed")
     torch.cuda.synchronize()
     launches0 = _lib.lib().ttgb_launch_count()
     sampler = ClockSampler(local)
@@ -223,90 +241,163 @@ def run_gb300(args):
         dist.barrier()
     torch.cuda.synchronize()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
-    t_start = torch.cuda.Event(enable_timing=True)
-    t_end = torch.cuda.Event(enable_timing=True)
-    t_start.record(stream)
-    stats = []
-    last = None
+    lat, results = [], None
     for i in range(args.steps):
-        flush.fill_(float(i))            # L2 flush between solves (256 MiB > 129 MB L2)
+        flush.fill_(float(i))            # L2 flush between steps (256 MiB > 129 MB L2)
         ev[2 * i].record(stream)
-        last, st = solve()
+        results = batch("mixed")
         ev[2 * i + 1].record(stream)
-        stats.append(st)
-    t_end.record(stream)
+        lat.extend(st["queue_ms"] + st["run_ms"] for _, st in results)
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
     clocks = sampler.stop()
     launches = _lib.lib().ttgb_launch_count() - launches0
-    elapsed_ms = t_start.elapsed_time(t_end)
-    lat = [ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(args.steps)]
+    step_ms = [ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(args.steps)]
+    elapsed_ms = sum(step_ms)
     if ws > 1:
         t = torch.tensor([elapsed_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed_ms = float(t.item())
-    value = ws * args.steps / (elapsed_ms / 1000.0)
+    value = ws * nb * args.steps / (elapsed_ms / 1000.0)
 
-    # relative residual of the last solution (TT algebra on the device)
-    A_tt, b_tt = TT(A_d), TT(b_d)
-    relres = float((A_tt @ TT(last) - b_tt).norm() / b_tt.norm())
+    # ---- the plain FP64 path, one solve at a time (the comparison point) ------------------------
+    fp64_ms, x_fp64 = [], None
+    for j in range(args.fp64_solves):
+        flush.fill_(0.5)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        xc, _ = single("fp64", j)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fp64_ms.append(e0.elapsed_time(e1))
+        if j == 0:
+            x_fp64 = TT(xc)
+    fp64_value = 1000.0 / statistics.mean(fp64_ms)
 
-    # live roofline of the dominant kernel (the FP64 contraction engine), one profiled solve
-    _, pst = solve(profile=1)
-    achieved = pst["contract_flops"] / (pst["contract_ms"] * 1e-3) / 1e12 if pst["contract_ms"] > 0 else None
-    per_launch_flops = pst["contract_flops"] / max(1, pst["contract_launches"])
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                "frac": (achieved / FP64_PEAK_TFLOPS) if achieved else None,
-                "traffic": read_traffic("contract_f64_laplace_potential_d20_n64.md"),
-                "kernel": "contract_kernel (FP64 contraction engine)",
-                "launches": pst["contract_launches"], "avg_launch_us": 1000 * pst["contract_ms"] / max(1, pst["contract_launches"]),
-                "flops_per_launch": per_launch_flops,
-                "peak_source": "measured FP64 FMA rate (profiles/fp64_fma_peak.md); MEASURED_PEAKS.json has no FP64 entry"}
+    # ---- the mixed path unbatched, and the FP64 path batched ------------------------------------
+    flush.fill_(0.25)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    xm_c, mixed_stats = single("mixed", 0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    mixed_single_ms = e0.elapsed_time(e1)
+    e0.record(stream)
+    fp64_batch = batch("fp64")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp64_batch_ms = e0.elapsed_time(e1)
 
-    # end to end through the public API with host-resident TT cores
-    A_h, b_h = TT([c.clone() for c in wl["A"]]), TT([c.clone() for c in wl["b"]])
-    x0_h = TT(wl["x0"]) if wl.get("x0") is not None else None
-    h2d = sum(c.numel() * 8 for c in wl["A"]) + sum(c.numel() * 8 for c in wl["b"]) + \
-        (sum(c.numel() * 8 for c in wl["x0"]) if wl.get("x0") is not None else 0)
-    e2e_steps = max(1, min(args.steps, 3))
+    # ---- accuracy of the timed solutions (TT algebra on the device) -----------------------------
+    def relres(x, b):
+        return float((A_d @ x - b).norm() / b.norm())
+
+    res_mixed = [relres(x, b) for (x, _), b in zip(results, bs_d)]
+    res_fp64 = relres(x_fp64, bs_d[0])
+    x_m0 = results[0][0]
+    dx = float((x_m0 - x_fp64).norm() / x_fp64.norm())
+
+    # ---- live roofline of the dominant kernels (one profiled solve of each path) ----------------
+    peaks = measured_peaks()
+    fp64_peak = ops.calibrate_fma("fp64")
+    fp32_peak = ops.calibrate_fma("fp32")
+    _, pm = single("mixed", 0, profile=True)
+    _, pf = single("fp64", 0, profile=True)
+    tc = engine in ("auto", "tc")
+    lowp_tflops = pm["lowp_flops"] / (pm["lowp_ms"] * 1e-3) / 1e12 if pm["lowp_ms"] > 0 else None
+    if tc:
+        peak = peaks.get("bf16_tflops_sustained") or 1700.0
+        roofline = {
+            "bound": "tensor", "achieved": lowp_tflops, "peak": peak, "unit": "TFLOP/s",
+            "frac": lowp_tflops / peak if lowp_tflops else None,
+            "traffic": read_profile_value("tc_gemm_d20_n64_local.md", "traffic_bytes_per_launch"),
+            "kernel": "low-precision local product: tc_gemm_kernel x3 (tcgen05.mma kind::tf32, 3xTF32 "
+                      "split) + operand gather",
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
+                           if "bf16_tflops_sustained" in peaks else "fallback 1.7 PF/s sustained",
+            "tf32_pipe_frac": 3 * lowp_tflops / (peak / 2) if lowp_tflops else None,
+        }
+    else:
+        roofline = {
+            "bound": "fp32-fma", "achieved": lowp_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": lowp_tflops / fp32_peak if lowp_tflops else None, "traffic": None,
+            "kernel": "low-precision local product: contract_kernel<float> x3 + casts",
+            "peak_source": "FP32 FMA pipe measured live (ttgb_calibrate_fma)",
+        }
+    roofline.update({
+        "launches": pm["lowp_launches"], "ms": pm["lowp_ms"],
+        "avg_launch_us": 1000 * pm["lowp_ms"] / max(1, pm["lowp_launches"]),
+        "flops_per_product": pm["lowp_flops"] / max(1, pm["lowp_matvecs"]),
+        "share_of_solve": pm["lowp_ms"] / max(1e-9, sum(pm["phase_ms"].values())),
+    })
+    fp64_tflops = pf["contract_flops"] / (pf["contract_ms"] * 1e-3) / 1e12 if pf["contract_ms"] > 0 else None
+    fp64_roof = {"kernel": "contract_kernel<double> (FP64 contraction engine, plain path)",
+                 "achieved": fp64_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
+                 "frac": fp64_tflops / fp64_peak if fp64_tflops else None,
+                 "peak_source": "FP64 FMA pipe measured live (ttgb_calibrate_fma)",
+                 "traffic": read_profile_value("contract_f64_laplace_potential_d20_n64.md",
+                                               "traffic_bytes_per_launch"),
+                 "launches": pf["contract_launches"],
+                 "avg_launch_us": 1000 * pf["contract_ms"] / max(1, pf["contract_launches"])}
+
+    # ---- end to end through the public API with host-resident inputs -----------------------------
+    A_h = TT([c.clone().pin_memory() for c in wls[0]["A"]])
+    bs_h = [TT([c.clone().pin_memory() for c in w["b"]]) for w in wls]
+    h2d = nb * sum(c.numel() * 8 for c in A_h.cores) + sum(c.numel() * 8 for b in bs_h for c in b.cores)
+    e2e_steps = max(1, min(args.steps, 2))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d2h = 0
     for _ in range(e2e_steps):
-        xh = amen_solve(A_h, b_h, x0=x0_h, **kw)
-        d2h = sum(c.numel() * 8 for c in xh.cores)
-    torch.cuda.synchronize()
+        out = batch("mixed", A=A_h, rhs=bs_h)
+        assert all(x.cores[0].device.type == "cpu" for x, _ in out)
+        d2h = sum(c.numel() * 8 for x, _ in out for c in x.cores)
     e2e_s = time.perf_counter() - t0
-    e2e_val = ws * e2e_steps / e2e_s if ws == 1 else None
     if ws > 1:
         t = torch.tensor([e2e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_val = ws * e2e_steps / float(t.item())
+        e2e_s = float(t.item())
+    e2e_val = ws * nb * e2e_steps / e2e_s
+    srv_stats = srv.stats()
+    srv.close()
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        dt, info = cpu_solve_once(wl)
+        dt, info = cpu_solve_once(wls[0])
         cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": "1 full solve of %s with the numpy restatement of the reference (oracle/amen.py), "
-                         "numpy/OpenBLAS threads = all host cores" % args.workload}
+               "sample": "1 full solve of %s (b seed %d) with the numpy restatement of the reference "
+                         "(oracle/amen.py), numpy/OpenBLAS threads = all host cores"
+                         % (args.workload, seeds[0])}
 
     if rank == 0:
-        st = stats[-1]
+        cfg = workload_config(args, wls[0])
+        cfg.update({"precision": "mixed", "engine": engine, "batch": nb, "server_slots": nb,
+                    "l2": "256 MiB flush write between steps",
+                    "parallelism": "replicas" if ws > 1 else "single"})
         line = {
-            "metric": "AMEn solves/s (single large solve, plain FP64 GPU path)",
-            "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": args.workload, "d": 20 if "d20" in args.workload else 8,
-                       "eps": p["eps"], "kickrank": p["kickrank"], "nswp": p.get("nswp", 22),
-                       "precision": "fp64", "l2": "256 MiB flush write between solves",
-                       "parallelism": "replicas" if ws > 1 else "single"},
-            "latency_ms": {"p50": percentile(lat, 0.5), "p99": percentile(lat, 0.99)},
-            "solve": {"relres": relres, "sweeps": st["sweeps"], "max_rank": max(st["ranks"]),
-                      "matvecs": st["matvecs"], "gmres_iterations": st["gmres_iterations"],
-                      "host_syncs": st["host_syncs"]},
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+tf32" if tc else "f64+f32",
+            "data": "synthetic (seeded)", "config": cfg,
+            "latency_ms": {"p50": percentile(lat, 0.5), "p99": percentile(lat, 0.99),
+                           "requests": len(lat)},
+            "fp64_plain": {"value": fp64_value, "unit": "solves/s", "ms_per_solve": statistics.mean(fp64_ms),
+                           "solves": len(fp64_ms), "relres": res_fp64},
+            "speedup_vs_fp64_plain": value / fp64_value,
+            "mixed_single": {"ms_per_solve": mixed_single_ms, "value": 1000.0 / mixed_single_ms,
+                             "refinements": mixed_stats["refinements"],
+                             "lowp_matvecs": mixed_stats["lowp_matvecs"], "matvecs": mixed_stats["matvecs"]},
+            "fp64_batched": {"value": 1000.0 * nb / fp64_batch_ms, "unit": "solves/s", "ms_per_step": fp64_batch_ms},
+            "accuracy": {"relres_max": max(res_mixed), "relres_fp64": res_fp64,
+                         "x_mixed_vs_fp64": dx, "eps": p["eps"]},
+            "solve": {"sweeps": mixed_stats["sweeps"], "max_rank": max(mixed_stats["ranks"]),
+                      "gmres_iterations": mixed_stats["gmres_iterations"],
+                      "host_syncs": mixed_stats["host_syncs"]},
+            "server": {"peak_running": srv_stats.get("peak_running"), "completed": srv_stats.get("completed")},
             "roofline": roofline,
+            "fp64_contract_roofline": fp64_roof,
+            "phase_ms_mixed": pm["phase_ms"],
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
@@ -326,6 +417,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=WORKLOADS[0], choices=WORKLOADS)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--engine", default="auto", choices=["auto", "tc", "fp32"])
+    ap.add_argument("--fp64-solves", type=int, default=2)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -147,6 +147,20 @@ int ttgb_server_stats(const ttgb_server* srv, int64_t* submitted, int64_t* compl
 /* Finishes queued and running requests, then frees the server. */
 void ttgb_server_destroy(ttgb_server* srv);
 
+/* ---- TT-level operations (FP64, device cores; a TT-matrix when x->rows is set) ---- */
+
+/* y = A x for a TT-matrix A and a TT-vector x (ranks multiply); the result is a library-owned
+   ttgb_solution. (replaces TT.__matmul__, torchtt/_tt_base.py:807-817) */
+int ttgb_tt_matvec(const ttgb_tt* A, const ttgb_tt* x, void* stream, ttgb_solution** out);
+/* ||x||_F by a QR sweep (replaces TT.norm, torchtt/_tt_base.py:1021-1051). */
+int ttgb_tt_norm(const ttgb_tt* x, double* out, void* stream);
+/* TT rounding to relative accuracy eps with rank cap rmax; the result is a library-owned
+   ttgb_solution (read with ttgb_solution_dims / _copy_core, free with ttgb_solution_free; a
+   TT-matrix core comes back as r x (m n) x R). (replaces TT.round / round_tt,
+   torchtt/_tt_base.py:1427-1450, torchtt/_decomposition.py:169-228; round_this,
+   cpp/compression.h:3-42) */
+int ttgb_tt_round(const ttgb_tt* x, double eps, int64_t rmax, void* stream, ttgb_solution** out);
+
 /* ---- kernel-level entry points (FP64, device pointers, workspace allocated internally) ---- */
 
 /* y[l,m,L] = sum Phi_l[l,s,r] A[s,m,n,S] Phi_r[L,S,R] x[r,n,R]

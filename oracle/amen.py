@@ -498,9 +498,11 @@ def tt_add(x_cores, y_cores, alpha=1.0, beta=1.0):
 
 
 def tt_norm(cores):
-    """Frobenius norm by a left-to-right QR sweep (torchtt/_tt_base.py:1021-1051)."""
+    """Frobenius norm by a left-to-right QR sweep (torchtt/_tt_base.py:1021-1051); TT-matrix
+    cores (4-D) are handled as r x (m n) x R."""
     cur = None
     for c in cores:
+        c = c.reshape(c.shape[0], -1, c.shape[-1])
         if cur is not None:
             c = np.tensordot(cur, c, axes=([1], [0]))
         mat = c.reshape(-1, c.shape[2])
@@ -526,3 +528,50 @@ def tt_relres(A_cores, x_cores, b_cores):
 def tt_relerr(x_cores, y_cores):
     """||x - y|| / ||y|| in the TT format."""
     return tt_norm(tt_add(x_cores, y_cores, 1.0, -1.0)) / tt_norm(y_cores)
+
+
+# --------------------------------------------------------------------------------------------------
+# TT rounding (torchtt/_decomposition.py:62-113,169-228,289-324)
+# --------------------------------------------------------------------------------------------------
+
+def rank_chop(s, tol):
+    """Smallest rank r >= 1 whose discarded tail sum_{k >= r} s_k^2 is below tol^2
+    (restates rank_chop, torchtt/_decomposition.py:289-324)."""
+    s = np.asarray(s, dtype=np.float64)
+    if np.linalg.norm(s) == 0.0:
+        return 1
+    if tol <= 0.0:
+        return s.size
+    tail = np.cumsum((s ** 2)[::-1])[::-1]
+    below = np.nonzero(tail < tol ** 2)[0]
+    if below.size == 0:
+        return s.size
+    return max(int(below[0]), 1)
+
+
+def tt_round(cores, eps, rmax=2 ** 62):
+    """TT rounding: left-to-right QR orthogonalisation (lr_orthogonal,
+    torchtt/_decomposition.py:62-113), then right-to-left truncated SVDs with threshold
+    eps / sqrt(d - 1) times the norm of each core's singular values and the rank cap rmax
+    (round_tt, torchtt/_decomposition.py:169-228). TT-matrix cores (4-D) are handled as
+    r x (m n) x R. Returns the new cores with the input's core shapes."""
+    shapes = [c.shape for c in cores]
+    cs = [c.reshape(c.shape[0], -1, c.shape[-1]).copy() for c in cores]
+    d = len(cs)
+    if d == 1:
+        return [c.copy() for c in cores]
+    for i in range(d - 1):
+        r, m, R = cs[i].shape
+        q, rf = np.linalg.qr(cs[i].reshape(r * m, R))
+        cs[i] = q.reshape(r, m, q.shape[1])
+        nxt = cs[i + 1]
+        cs[i + 1] = (rf @ nxt.reshape(nxt.shape[0], -1)).reshape(rf.shape[0], nxt.shape[1], nxt.shape[2])
+    ep = eps / math.sqrt(d - 1)
+    for i in range(d - 1, 0, -1):
+        r, m, R = cs[i].shape
+        u, s, vh = np.linalg.svd(cs[i].reshape(r, m * R), full_matrices=False)
+        rn = min(int(rmax), rank_chop(s, np.linalg.norm(s) * ep))
+        cs[i] = vh[:rn].reshape(rn, m, R)
+        prev = cs[i - 1]
+        cs[i - 1] = (prev.reshape(-1, r) @ (u[:, :rn] * s[:rn])).reshape(prev.shape[0], prev.shape[1], rn)
+    return [c.reshape((c.shape[0],) + tuple(sh[1:-1]) + (c.shape[-1],)) for c, sh in zip(cs, shapes)]

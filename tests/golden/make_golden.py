@@ -8,6 +8,7 @@ Python package is imported from the tree. Writes ``tests/golden/*.npz``:
   updates (``torchtt/solvers.py:36-68,691-775``, the Python twins of ``cpp/amen_solve.h:17-98``) on
   seeded random shapes, plus a GMRES known answer (``torchtt/_iterative_solvers.py:72-158`` on a
   1-D Laplacian, the pattern of ``cpp/test_gmres.cpp:187-253``);
+* ``round.npz`` - inputs and outputs of the reference's TT rounding (``TT.round``);
 * ``solve_<name>.npz`` - the inputs of a whole solve (A, b, x0 cores, the initial enrichment cores z0
   that the reference drew with ``torch::randn`` after ``torch.manual_seed``), the parameters, and the
   solution cores returned by ``torchttcpp.amen_solve`` (``cpp/amen_solve.h:122``) and, for the small
@@ -88,6 +89,32 @@ def kernels(torchtt):
     print("kernels.npz written")
 
 
+def rounding(torchtt):
+    """TT rounding by the reference's ``TT.round`` (torchtt/_tt_base.py:1427-1450) on inputs with
+    decaying and with flat rank spectra, a rank cap, a TT-matrix and d = 1."""
+    def wsum(N, r, seed, weights):
+        acc = None
+        for i, w in enumerate(weights):
+            t = torchtt.TT(W.random_tt(N, [1] + [r] * (len(N) - 1) + [1], seed + i)) * w
+            acc = t if acc is None else acc + t
+        return acc
+    decay = wsum([5] * 6, 6, 31, [1.0, 1e-3, 1e-6, 1e-9])
+    flat = wsum([6] * 8, 16, 41, [1.0, 1.0, 1.0, 1.0])
+    lap = torchtt.TT(W.laplace_ttm(4, 5))
+    cases = [("decay_eps1e-7", decay, 1e-7, 2 ** 62), ("decay_rmax7", decay, 1e-12, 7),
+             ("flat_eps1e-8", flat, 1e-8, 2 ** 62), ("ttm_sum", lap + lap, 1e-12, 2 ** 62),
+             ("d1", torchtt.TT(W.random_tt([9], [1, 1], 51)), 1e-8, 2 ** 62)]
+    out = {"names": np.array([c[0] for c in cases])}
+    for name, x, eps, rmax in cases:
+        y = x.round(eps, rmax)
+        _pack_cores(name + "_in", x.cores, out)
+        _pack_cores(name + "_out", y.cores, out)
+        out[name + "_eps"] = np.array(eps)
+        out[name + "_rmax"] = np.array(rmax, dtype=np.int64)
+    np.savez_compressed(os.path.join(HERE, "round.npz"), **out)
+    print("round.npz written")
+
+
 def solve_case(torchtt, cpp, wl, seed, prec=None, with_python=False, extra=None):
     A, b, x0 = wl["A"], wl["b"], wl.get("x0")
     p = dict(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
@@ -139,6 +166,7 @@ def main():
     torch.set_num_threads(max(1, os.cpu_count() or 1))
     torchtt, cpp = build_ref.load_reference_package()
     kernels(torchtt)
+    rounding(torchtt)
     small = W.small_random_system(0)
     for prec in (None, "c", "r"):
         solve_case(torchtt, cpp, small, seed=11, prec=prec, with_python=True,

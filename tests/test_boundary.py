@@ -48,8 +48,22 @@ def test_no_cpu_fallback():
         amen_solve(A, b)
 
 
-def test_tt_algebra_on_cpu():
+def test_tt_sub_on_cpu():
+    """x - b concatenates cores; the difference of b with itself has norm 0 (oracle check)."""
+    from oracle import amen as O
+    wl = W.small_random_system(0)
+    b = TT(wl["b"])
+    res = [c.numpy() for c in (b - b).cores]
+    assert O.tt_norm(res) < 1e-14 * O.tt_norm([c.numpy() for c in b.cores])
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU behaviour")
+def test_tt_algebra_needs_gpu():
     wl = W.small_random_system(0)
     A, x, b = TT(wl["A"]), TT(wl["x"]), TT(wl["b"])
-    r = (A @ x - b).norm() / b.norm()
-    assert float(r) < 1e-12
+    with pytest.raises(RuntimeError):
+        b.norm()
+    with pytest.raises(RuntimeError):
+        A @ x
+    with pytest.raises(RuntimeError):
+        b.round(1e-8)

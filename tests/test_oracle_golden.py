@@ -58,3 +58,26 @@ def test_tt_helpers():
     assert abs(O.tt_norm(cores) - np.linalg.norm(full)) <= 1e-12 * np.linalg.norm(full)
     diff = O.tt_add(cores, cores, 1.0, -1.0)
     assert O.tt_norm(diff) <= 1e-12 * np.linalg.norm(full)
+
+
+def _round_cases():
+    z = G.load("round.npz")
+    for name in z["names"]:
+        name = str(name)
+        yield (name, G.cores(z, name + "_in"), G.cores(z, name + "_out"), float(z[name + "_eps"]),
+               int(z[name + "_rmax"]))
+
+
+def test_round_matches_reference():
+    """TT rounding of the oracle against the reference's TT.round: same ranks, same tensor."""
+    for name, xin, xref, eps, rmax in _round_cases():
+        y = O.tt_round(xin, eps, rmax)
+        assert [c.shape for c in y] == [c.shape for c in xref], name
+        diff = O.tt_norm(O.tt_add([c.reshape(c.shape[0], -1, c.shape[-1]) for c in y],
+                                  [c.reshape(c.shape[0], -1, c.shape[-1]) for c in xref], 1.0, -1.0))
+        assert diff <= 1e-12 * O.tt_norm(xref), (name, diff)
+        # the rounding error itself stays within eps (rank-capped cases excepted)
+        if rmax > 1000:
+            err = O.tt_norm(O.tt_add([c.reshape(c.shape[0], -1, c.shape[-1]) for c in y],
+                                     [c.reshape(c.shape[0], -1, c.shape[-1]) for c in xin], 1.0, -1.0))
+            assert err <= eps * O.tt_norm(xin) * 1.0001, (name, err)

@@ -59,17 +59,6 @@ __global__ void assemble_dense_kernel(const double* __restrict__ phil, const dou
   }
 }
 
-// X (rows x cols, column-major, ld) : X[q + j*ld] *= S[q]
-__global__ void scale_rows_cm_kernel(double* X, int64_t ld, int64_t rows, int64_t cols,
-                                     const double* S) {
-  const int64_t total = rows * cols;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t q = t % rows, j = t / rows;
-    X[q + j * ld] *= S[q];
-  }
-}
-
 unsigned grid_of(int64_t n) {
   unsigned g = cdiv(n, 256);
   const unsigned cap = 8 * (unsigned)num_sms();
@@ -605,8 +594,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
     DBuf Mc((size_t)(a * bdim), s_), U((size_t)(a * kf), s_), S((size_t)kf, s_), SVh((size_t)(kf * bdim), s_);
     transpose(sol.p, bdim, Mc.p, a, bdim, a, s_);
     svd(Mc.p, a, a, bdim, U.p, S.p, SVh.p, lws_, red_, s_);
-    scale_rows_cm_kernel<<<grid_of(kf * bdim), 256, 0, s_>>>(SVh.p, kf, kf, bdim, S.p);
-    TTGB_CHECK_LAUNCH();
+    scale_rows_cm(SVh.p, kf, kf, bdim, S.p, s_);
     phase(kPhFwdRank);
     const double thr = res_new > real_tol * damp ? res_new : real_tol * damp;
     int64_t r = (mixed_ && !use_full)

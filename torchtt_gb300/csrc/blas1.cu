@@ -382,6 +382,25 @@ void transpose(const double* src, int64_t sld, double* dst, int64_t dld, int64_t
   TTGB_CHECK_LAUNCH();
 }
 
+namespace {
+__global__ void scale_rows_cm_kernel(double* X, int64_t ld, int64_t rows, int64_t cols,
+                                     const double* S) {
+  const int64_t total = rows * cols;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = t % rows, j = t / rows;
+    X[q + j * ld] *= S[q];
+  }
+}
+}  // namespace
+
+void scale_rows_cm(double* X, int64_t ld, int64_t rows, int64_t cols, const double* S,
+                   cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return;
+  scale_rows_cm_kernel<<<ew_grid(rows * cols), 256, 0, s>>>(X, ld, rows, cols, S);
+  TTGB_CHECK_LAUNCH();
+}
+
 void combine(const double* Q, int64_t ldq, int k, const double* c, const double* y0, double* y,
              int64_t n, cudaStream_t s) {
   if (n <= 0) return;

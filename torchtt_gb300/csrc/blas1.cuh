@@ -44,6 +44,9 @@ void copy2d(const double* src, int64_t sld, double* dst, int64_t dld, int64_t ro
 // dst (rows x cols, row-major ld) = transpose of src (cols x rows, row-major sld)
 void transpose(const double* src, int64_t sld, double* dst, int64_t dld, int64_t rows, int64_t cols,
                cudaStream_t s);
+// X (rows x cols, column-major, ld): X[q + j*ld] *= S[q]  (S device)
+void scale_rows_cm(double* X, int64_t ld, int64_t rows, int64_t cols, const double* S,
+                   cudaStream_t s);
 // precision casts
 void cast(const double* x, float* y, int64_t n, cudaStream_t s);
 void cast(const float* x, double* y, int64_t n, cudaStream_t s);

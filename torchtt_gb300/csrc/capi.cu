@@ -1,6 +1,7 @@
 // extern "C" surface of the library (declared in include/ttgb300.h). Every entry point converts
 // exceptions into status codes and keeps the message in a thread-local buffer.
 #include <cstring>
+#include <memory>
 #include <string>
 
 #include "../../include/ttgb300.h"
@@ -13,6 +14,7 @@
 #include "prec.cuh"
 #include "tc_gemm.cuh"
 #include "tc_local.cuh"
+#include "tt_ops.cuh"
 
 using namespace ttgb;
 
@@ -214,6 +216,42 @@ int ttgb_solution_copy_core(const ttgb_solution* sol, int32_t k, double* dst, in
 }
 
 void ttgb_solution_free(ttgb_solution* sol) { delete sol; }
+
+int ttgb_tt_matvec(const ttgb_tt* A, const ttgb_tt* x, void* stream, ttgb_solution** out) {
+  return guarded([&] {
+    TTGB_REQUIRE(A && x && out && A->d > 0 && A->d == x->d, "bad TT matvec arguments");
+    TTGB_REQUIRE(A->rows != nullptr && x->rows == nullptr,
+                 "Only TT-matrix @ TT-vector is supported here.");
+    const TTView va = view_of(A, true), vx = view_of(x, false);
+    cudaStream_t s = as_stream(stream);
+    std::unique_ptr<ttgb_solution> sol(new ttgb_solution());
+    sol->res.cores = tt_matvec(va, vx, s, sol->res.ranks);
+    TTGB_CUDA(cudaStreamSynchronize(s));
+    *out = sol.release();
+  });
+}
+
+int ttgb_tt_norm(const ttgb_tt* x, double* out, void* stream) {
+  return guarded([&] {
+    TTGB_REQUIRE(x != nullptr && x->d > 0 && out != nullptr, "bad TT norm arguments");
+    const TTView v = view_of(x, x->rows != nullptr);
+    Scratch sc(as_stream(stream));
+    *out = tt_norm(v, sc.lws, sc.red, sc.s);
+  });
+}
+
+int ttgb_tt_round(const ttgb_tt* x, double eps, int64_t rmax, void* stream, ttgb_solution** out) {
+  return guarded([&] {
+    TTGB_REQUIRE(x != nullptr && x->d > 0 && out != nullptr, "bad TT round arguments");
+    TTGB_REQUIRE(rmax >= 1, "rmax must be positive");
+    const TTView v = view_of(x, x->rows != nullptr);
+    Scratch sc(as_stream(stream));
+    std::unique_ptr<ttgb_solution> sol(new ttgb_solution());
+    sol->res.cores = tt_round(v, eps, rmax, sc.lws, sc.red, sc.s, sol->res.ranks);
+    TTGB_CUDA(cudaStreamSynchronize(sc.s));
+    *out = sol.release();
+  });
+}
 
 int ttgb_local_product(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, int64_t S,
                        int64_t RL, int64_t R, const double* phi_l, const double* A,

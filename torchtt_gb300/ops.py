@@ -143,3 +143,11 @@ def local_product_lowp(Phi_right, Phi_left, coreA, core, engine=ENGINE_TC):
                                                   _ptr(Phi_right), _ptr(core), _ptr(y), int(engine),
                                                   _stream(core.device)))
     return y
+
+
+def calibrate_fma(dtype="fp64"):
+    """Measured peak of this GPU's FMA pipe in TFLOP/s for ``dtype`` 'fp64' or 'fp32'
+    (independent FMA chains on every SM; about 0.2 s)."""
+    out = ctypes.c_double()
+    _lib.check(_lib.lib().ttgb_calibrate_fma({"fp64": 0, "fp32": 1}[dtype], ctypes.byref(out)))
+    return out.value

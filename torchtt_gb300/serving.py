@@ -25,7 +25,10 @@ class Server:
     def __init__(self, slots=8, mem_budget_bytes=0, device=None):
         if not torch.cuda.is_available():
             raise RuntimeError("the gb300 server needs a CUDA device")
-        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        if isinstance(device, torch.device):
+            self.device = device
+        else:
+            self.device = torch.device("cuda", torch.cuda.current_device() if device is None else int(device))
         torch.cuda.set_device(self.device)
         self._L = _lib.lib()
         h = _lib.c_vp()

@@ -63,20 +63,10 @@ def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-
     db = _desc(b_cores, False, keep)
     dx = _desc(x0_cores, False, keep) if x0_cores else None
     dz = _desc(z0_cores, False, keep) if z0_cores else None
-    p = _lib.AmenParams()
-    L.ttgb_default_params(ctypes.byref(p))
-    p.nswp, p.eps, p.rmax, p.max_full = int(nswp), float(eps), int(rmax), int(max_full)
-    p.kickrank, p.kick2 = int(kickrank), int(kick2)
-    p.local_iterations, p.resets = int(local_iterations), int(resets)
-    p.verbose, p.preconditioner, p.seed = int(bool(verbose)), int(preconditioner), int(seed)
-    if precision not in _lib.PRECISION:
-        raise InvalidArguments("precision must be 'fp64' or 'mixed'")
-    p.precision = _lib.PRECISION[precision]
-    p.profile = int(bool(profile))
-    engines = {"auto": 0, "fp32": 1, "tc": 2}
-    if engine not in engines:
-        raise InvalidArguments("engine must be 'auto', 'fp32' or 'tc'")
-    p.lowp_engine = engines[engine]
+    p = make_params(nswp=nswp, eps=eps, rmax=rmax, max_full=max_full, kickrank=kickrank,
+                    kick2=kick2, local_iterations=local_iterations, resets=resets, verbose=verbose,
+                    preconditioner=preconditioner, seed=seed, precision=precision, profile=profile,
+                    engine=engine)
     if stream is None:
         stream = torch.cuda.current_stream(A_cores[0].device)
     handle = _lib.c_vp()
@@ -137,7 +127,8 @@ def make_params(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=
 def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
                trunc_norm='res', local_solver=1, local_iterations=40, resets=2, verbose=False,
                preconditioner=None, use_cpp=True, band_diagonal=-1, use_single_precision=False,
-               backend='gb300', seed=1, z0=None, return_stats=False, precision=None):
+               backend='gb300', seed=1, z0=None, return_stats=False, precision=None,
+               engine='auto'):
     """Solve the multilinear system A x = b in the TT format with AMEn on the GPU.
 
     Arguments are those of ``torchtt.solvers.amen_solve`` (``torchtt/solvers.py:211``), with the same
@@ -150,7 +141,9 @@ def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kick
     * ``return_stats``: also return a dict of solver statistics;
     * ``precision``: ``'fp64'`` (the reference's arithmetic) or ``'mixed'`` (low-precision local
       GMRES operator inside FP64 iterative refinement). ``use_single_precision=True``, the
-      reference's own mixed mode (``torchtt/solvers.py:469-496``), selects ``'mixed'``.
+      reference's own mixed mode (``torchtt/solvers.py:469-496``), selects ``'mixed'``;
+    * ``engine``: low-precision contraction engine of the mixed path, ``'auto'`` (tcgen05 when
+      available), ``'tc'`` (tcgen05 3xTF32 tensor cores) or ``'fp32'`` (FP32 CUDA cores).
     """
     # argument checks of torchtt/solvers.py:259-266
     if not (_is_tt(A) and _is_tt(b)):
@@ -177,7 +170,7 @@ def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kick
     cores, stats = solve_cores(Ac, bc, xc, zc, nswp=nswp, eps=eps, rmax=rmax, max_full=max_full,
                                kickrank=kickrank, kick2=kick2, local_iterations=local_iterations,
                                resets=resets, verbose=verbose, preconditioner=_PREC[preconditioner],
-                               seed=seed,
+                               seed=seed, engine=engine,
                                precision=precision or ("mixed" if use_single_precision else "fp64"))
     cores = [c.to(device=out_device, dtype=out_dtype) for c in cores]
     cls = type(b) if _is_tt(b) else TT

@@ -2,8 +2,10 @@
 
 ``TT`` mirrors the parts of the reference's ``torchtt.TT`` (``torchtt/_tt_base.py:18-229``) that
 the AMEn path uses: construction from a list of cores with the same rank checks and errors, the
-``cores``/``N``/``M``/``R``/``is_ttm`` properties, device moves, and the algebra the reference's
-tests apply to a solution (``A @ x``, ``x - b``, ``.norm()``; ``tests/test_solvers.py:19``).
+``cores``/``N``/``M``/``R``/``is_ttm`` properties, device moves, the algebra the reference's
+tests apply to a solution (``A @ x``, ``x - b``, ``.norm()``; ``tests/test_solvers.py:19``) and
+``round``. ``@``, ``norm`` and ``round`` run on the GPU through the library; ``+``/``-`` only
+concatenate cores.
 The solver also accepts the reference's own ``torchtt.TT`` objects (anything with ``cores`` and
 ``is_ttm``) and returns an object of the same class as ``b``.
 """
@@ -80,16 +82,25 @@ class TT:
 
     # -- algebra used to check solutions ------------------------------------------------------
     def __matmul__(self, other):
-        """TT-matrix @ TT-vector core by core (torchtt/_tt_base.py:807-817): ranks multiply."""
+        """TT-matrix @ TT-vector core by core (torchtt/_tt_base.py:807-817): ranks multiply. Runs
+        on the GPU (``ttgb_tt_matvec``); the result lives on the device of ``other``'s cores."""
+        import ctypes
+        from . import _lib
+        from .solvers import _desc, fetch_solution
         if not (self._is_ttm and not other.is_ttm):
             raise IncompatibleTypes("Only TT-matrix @ TT-vector is supported here.")
         if self._N != list(other.N):
             raise ShapeMismatch("Shapes are incompatible.")
-        out = []
-        for a, c in zip(self.cores, other.cores):
-            t = torch.einsum("smnS,rnR->srmSR", a, c)
-            out.append(t.reshape(a.shape[0] * c.shape[0], a.shape[1], a.shape[3] * c.shape[2]))
-        return TT(out)
+        Ac, dev = self._device_cores()
+        xc = [c.detach().to(device=dev, dtype=torch.float64).contiguous() for c in other.cores]
+        keep = []
+        dA, dx = _desc(Ac, True, keep), _desc(xc, False, keep)
+        stream = torch.cuda.current_stream(dev)
+        h = _lib.c_vp()
+        _lib.check(_lib.lib().ttgb_tt_matvec(ctypes.byref(dA), ctypes.byref(dx),
+                                             ctypes.c_void_p(stream.cuda_stream), ctypes.byref(h)))
+        out, _ = fetch_solution(h, list(self._M), dev, stream)
+        return TT([c.to(other.cores[0].device) for c in out])
 
     def _combine(self, other, beta):
         if self._is_ttm or other.is_ttm:
@@ -126,19 +137,51 @@ class TT:
 
     __rmul__ = __mul__
 
-    def norm(self):
-        """Frobenius norm by a left-to-right QR sweep (torchtt/_tt_base.py:1021-1051).
+    def _device_cores(self):
+        """The cores as contiguous CUDA float64 tensors (copied to the current GPU if needed)."""
+        if not torch.cuda.is_available():
+            raise RuntimeError("TT products, norms and rounding run on the GPU; no CUDA device is "
+                               "available.")
+        dev = self.cores[0].device if self.cores[0].is_cuda else \
+            torch.device("cuda", torch.cuda.current_device())
+        return [c.detach().to(device=dev, dtype=torch.float64).contiguous() for c in self.cores], dev
 
-        A checking utility, not part of the solver: the small QR factorisations run on the CPU."""
-        cur = None
-        for c in self.cores:
-            c = c.detach().cpu()
-            if c.dim() == 4:
-                c = c.reshape(c.shape[0], c.shape[1] * c.shape[2], c.shape[3])
-            if cur is not None:
-                c = torch.tensordot(cur, c, dims=([1], [0]))
-            _, cur = torch.linalg.qr(c.reshape(-1, c.shape[-1]))
-        return torch.linalg.norm(cur)
+    def norm(self):
+        """Frobenius norm (torchtt/_tt_base.py:1021-1051), computed on the GPU by a QR sweep
+        (``ttgb_tt_norm``); returns a 0-d float64 tensor on the device of the cores."""
+        import ctypes
+        from . import _lib
+        from .solvers import _desc
+        cores, dev = self._device_cores()
+        keep = []
+        desc = _desc(cores, self._is_ttm, keep)
+        out = ctypes.c_double()
+        stream = torch.cuda.current_stream(dev)
+        _lib.check(_lib.lib().ttgb_tt_norm(ctypes.byref(desc), ctypes.byref(out),
+                                           ctypes.c_void_p(stream.cuda_stream)))
+        return torch.tensor(out.value, dtype=torch.float64, device=self.cores[0].device)
+
+    def round(self, eps=1e-12, rmax=2**62):
+        """TT rounding to relative accuracy ``eps`` with rank cap ``rmax`` (torchtt/_tt_base.py:
+        1427-1450, round_tt in torchtt/_decomposition.py:169-228) on the GPU (``ttgb_tt_round``).
+        Returns a new TT on the device of the cores."""
+        import ctypes
+        from . import _lib
+        from .solvers import _desc, fetch_solution
+        if isinstance(rmax, (list, tuple)):
+            raise InvalidArguments("rmax must be an integer here.")
+        cores, dev = self._device_cores()
+        keep = []
+        desc = _desc(cores, self._is_ttm, keep)
+        stream = torch.cuda.current_stream(dev)
+        h = _lib.c_vp()
+        _lib.check(_lib.lib().ttgb_tt_round(ctypes.byref(desc), float(eps), int(rmax),
+                                            ctypes.c_void_p(stream.cuda_stream), ctypes.byref(h)))
+        modes = [m * n for m, n in zip(self._M, self._N)] if self._is_ttm else list(self._N)
+        out, _ = fetch_solution(h, modes, dev, stream)
+        if self._is_ttm:
+            out = [c.reshape(c.shape[0], m, n, c.shape[2]) for c, m, n in zip(out, self._M, self._N)]
+        return TT([c.to(self.cores[0].device) for c in out])
 
     def full(self):
         t = self.cores[0]
