@@ -305,7 +305,7 @@ def run_gb300(args):
     _, pm = single("mixed", 0, profile=True)
     _, pf = single("fp64", 0, profile=True)
     tc = engine in ("auto", "tc")
-    lowp_tflops = pm["lowp_flops"] / (pm["lowp_ms"] * 1e-3) / 1e12 if pm["lowp_ms"] > 0 else None
+    lowp_tflops = pm["lowp_gemm_flops"] / (pm["lowp_ms"] * 1e-3) / 1e12 if pm["lowp_ms"] > 0 else None
     if tc:
         peak = peaks.get("bf16_tflops_sustained") or 1700.0
         roofline = {
@@ -328,7 +328,7 @@ def run_gb300(args):
     roofline.update({
         "launches": pm["lowp_launches"], "ms": pm["lowp_ms"],
         "avg_launch_us": 1000 * pm["lowp_ms"] / max(1, pm["lowp_launches"]),
-        "flops_per_product": pm["lowp_flops"] / max(1, pm["lowp_matvecs"]),
+        "gemm_flops_per_product": pm["lowp_gemm_flops"] / max(1, pm["lowp_matvecs"]),
         "share_of_solve": pm["lowp_ms"] / max(1e-9, sum(pm["phase_ms"].values())),
     })
     fp64_tflops = pf["contract_flops"] / (pf["contract_ms"] * 1e-3) / 1e12 if pf["contract_ms"] > 0 else None

@@ -66,6 +66,8 @@ typedef struct ttgb_amen_params {
   int32_t precision;            /* TTGB_PRECISION_FP64 (default) or TTGB_PRECISION_MIXED */
   int32_t lowp_engine;          /* MIXED only: 0 auto (TTGB_ENGINE_TC when available),
                                    TTGB_ENGINE_FP32 or TTGB_ENGINE_TC */
+  int32_t a_structure;          /* 1 (default): A cores with density < 1/4 (Kronecker-sum
+                                   operators) are applied from their nonzeros; 0: always dense */
 } ttgb_amen_params;
 
 /* Precision modes. FP64: the reference's arithmetic. MIXED: the local GMRES applies the projected
@@ -90,7 +92,8 @@ typedef struct ttgb_stats {
   int64_t host_syncs;
   double contract_ms;           /* profile only: device time of the contraction kernels */
   int64_t contract_launches;    /* profile only: number of contraction kernel launches */
-  double contract_flops;        /* profile only: algorithmic flops of those launches */
+  double contract_flops;        /* profile only: flops of those GEMM launches (an A stage applied
+                                   from the nonzeros of a sparse core is not counted) */
   int64_t lowp_matvecs;         /* mixed: low-precision local products */
   double lowp_flops;            /* mixed: their algorithmic flops */
   int64_t refinements;          /* mixed: FP64 refinement steps */
@@ -99,6 +102,7 @@ typedef struct ttgb_stats {
                                    search, forward z, enrichment, forward interfaces, other */
   double lowp_ms;               /* profile + mixed: device time of the low-precision products */
   int64_t lowp_launches;        /* profile + mixed: kernel launches of those products */
+  double lowp_gemm_flops;       /* profile + mixed: flops of their GEMM launches */
 } ttgb_stats;
 
 typedef struct ttgb_solution ttgb_solution;   /* opaque, library-owned result */

@@ -148,3 +148,37 @@ def test_local_gmres_vs_oracle(cuda, prec):
     assert flag == fo == 1
     assert abs(nit - no) <= 1
     close(x, xo, tol=1e-9)
+
+
+def _kron_core(k, d, n):
+    """One core of the Laplacian-plus-potential operator (rank 3, tridiagonal/diagonal blocks):
+    the sparse A cores the structured A stage applies from their nonzeros."""
+    from torchtt_gb300 import workloads as W
+    return W.laplace_potential_ttm(d, n)[k].numpy()
+
+
+@pytest.mark.parametrize("k", [0, 2, 4])
+@pytest.mark.parametrize("rR", [(7, 9), (40, 36)])
+def test_structured_a_stage(cuda, k, rR):
+    """Local product and both interface updates with a sparse A core (structured A stage) against
+    the oracle's dense contractions, FP64 and both low-precision engines."""
+    from torchtt_gb300 import ops
+    A = _kron_core(k, 5, 24)
+    s, n, _, S = A.shape
+    r, R = rR
+    g = np.random.default_rng(k * 100 + r)
+    PhiL, PhiR = g.standard_normal((r, s, r)), g.standard_normal((R, S, R))
+    x = g.standard_normal((r, n, R))
+    ref = O.local_product(PhiR, PhiL, A, x)
+    close(ops.local_product(t(PhiR, cuda), t(PhiL, cuda), t(A, cuda), t(x, cuda)), ref)
+    for engine in (1, 2):
+        y = ops.local_product_lowp(t(PhiR, cuda), t(PhiL, cuda), t(A, cuda), t(x, cuda),
+                                   engine=engine).cpu().numpy()
+        assert np.linalg.norm(y - ref) <= 1e-5 * np.linalg.norm(ref), engine
+    z = g.standard_normal((r + 1, n, R + 2))
+    Pf = g.standard_normal((r + 1, s, r))
+    close(ops.compute_phi_fwd_A(t(Pf, cuda), t(z, cuda), t(A, cuda), t(x, cuda)),
+          O.compute_phi_fwd_A(Pf, z, A, x))
+    Pb = g.standard_normal((R + 2, S, R))
+    close(ops.compute_phi_bck_A(t(Pb, cuda), t(z, cuda), t(A, cuda), t(x, cuda)),
+          O.compute_phi_bck_A(Pb, z, A, x))

@@ -110,3 +110,27 @@ def test_mixed_equals_fp64_on_laplace(cuda):
     assert rmx <= max(1e-9, 2 * r64), (rmx, r64)
     assert float((xmx - x64).norm() / x64.norm()) <= 1e-9
     assert smx["lowp_matvecs"] > 0 and smx["refinements"] > 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_structured_a_matches_dense(cuda, precision):
+    """The structured A stage (sparse Kronecker-sum cores) and the dense contraction give the same
+    solve within the solve tolerance, and both match the reference's solution."""
+    from torchtt_gb300 import TT, amen_solve
+    z = G.load("solve_laplace_d8_n16.npz")
+    A, b = G.cores(z, "A"), G.cores(z, "b")
+    x0, z0 = G.cores(z, "x0"), G.cores(z, "z0")
+    p = G.params(z)
+    At = TT([torch.from_numpy(c).to(cuda) for c in A])
+    bt = TT([torch.from_numpy(c).to(cuda) for c in b])
+    kw = dict(nswp=p["nswp"], eps=p["eps"], kickrank=p["kickrank"], precision=precision,
+              x0=TT([torch.from_numpy(c).to(cuda) for c in x0]),
+              z0=[torch.from_numpy(c).to(cuda) for c in z0])
+    xs, st = amen_solve(At, bt, return_stats=True, **kw)
+    from torchtt_gb300.solvers import solve_cores
+    xd, _ = solve_cores(At.cores, bt.cores, kw["x0"].cores, kw["z0"], nswp=p["nswp"], eps=p["eps"],
+                        kickrank=p["kickrank"], precision=precision, a_structure=False)
+    xd = TT(xd)
+    assert float((xs - xd).norm() / xd.norm()) <= 10 * p["eps"]
+    _parity.check(A, b, [c.cpu().numpy() for c in xs.cores], G.cores(z, "x_cpp"), p["eps"],
+                  p["kickrank"], label="structured " + precision)

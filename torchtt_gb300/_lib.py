@@ -30,7 +30,8 @@ class AmenParams(ctypes.Structure):
     _fields_ = [("nswp", c_i32), ("eps", c_dbl), ("rmax", c_i64), ("max_full", c_i64),
                 ("kickrank", c_i32), ("kick2", c_i32), ("local_iterations", c_i32),
                 ("resets", c_i32), ("verbose", c_i32), ("preconditioner", c_i32), ("seed", c_u64),
-                ("profile", c_i32), ("precision", c_i32), ("lowp_engine", c_i32)]
+                ("profile", c_i32), ("precision", c_i32), ("lowp_engine", c_i32),
+                ("a_structure", c_i32)]
 
 PRECISION = {"fp64": 0, "mixed": 1}
 
@@ -42,7 +43,8 @@ class Stats(ctypes.Structure):
                 ("other_flops", c_dbl), ("host_syncs", c_i64), ("contract_ms", c_dbl),
                 ("contract_launches", c_i64), ("contract_flops", c_dbl),
                 ("lowp_matvecs", c_i64), ("lowp_flops", c_dbl), ("refinements", c_i64),
-                ("phase_ms", c_dbl * 12), ("lowp_ms", c_dbl), ("lowp_launches", c_i64)]
+                ("phase_ms", c_dbl * 12), ("lowp_ms", c_dbl), ("lowp_launches", c_i64),
+                ("lowp_gemm_flops", c_dbl)]
 
     PHASES = ("bwd_z", "bwd_qr", "bwd_phi", "fwd_setup", "local_solve", "svd", "rank_search",
               "fwd_z", "enrichment", "fwd_phi", "other")

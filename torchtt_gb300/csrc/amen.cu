@@ -154,6 +154,7 @@ class AmenRun {
   FBuf phil32_, phir32_, xf_, yf_, w1f_, w2f_;
   bool use_tc_ = false;    // mixed path on the tcgen05 engine
   std::vector<TcCore> tc_cores_;
+  std::vector<SparseCore> spA_;   // nonzero structure of each A core (structured A stage)
   TcLocal tc_local_;
   int* tc_err_ = nullptr;
   DBuf resvec_;
@@ -184,8 +185,8 @@ class AmenRun {
     w1_.ensure(local_product_w1(dm), s_);
     w2_.ensure(local_product_w2(dm), s_);
     if (prof_) prof_->begin();
-    local_product(dm, phil, Acore(k), phir, x, y, w1_.p, w2_.p, s_, alpha, beta);
-    if (prof_) prof_->end(lp_flops(dm), 3);
+    local_product(dm, phil, Acore(k), phir, x, y, w1_.p, w2_.p, s_, alpha, beta, &spA_[k]);
+    if (prof_) prof_->end(local_product_gemm_flops(dm, &spA_[k]), 3);
     if (main_system) { st_.matvecs++; st_.matvec_flops += lp_flops(dm); }
     else st_.other_flops += lp_flops(dm);
   }
@@ -200,17 +201,21 @@ class AmenRun {
              const double* right, int64_t r, int64_t R, int k, DTensor& out) {
     PhiDims pd{l, L, rA_[k], rA_[k + 1], r, R, N_[k], N_[k]};
     wphi_.ensure(phi_A_workspace(pd), s_);
-    const double f = 2.0 * (fwd ? (double)l * rA_[k] * r * N_[k] * L + (double)r * L * N_[k] * rA_[k] * N_[k] * rA_[k + 1] +
+    // flops of the GEMM launches; the A stage counts only when it is a GEMM (dense core)
+    const double a_stage = spA_[k].use ? 0.0 : 1.0;
+    const double f = 2.0 * (fwd ? (double)l * rA_[k] * r * N_[k] * L +
+                                      a_stage * r * L * N_[k] * rA_[k] * N_[k] * rA_[k + 1] +
                                       (double)L * rA_[k + 1] * R * r * N_[k]
-                                 : (double)l * N_[k] * rA_[k + 1] * R * L + (double)l * R * rA_[k] * N_[k] * N_[k] * rA_[k + 1] +
+                                 : (double)l * N_[k] * rA_[k + 1] * R * L +
+                                      a_stage * l * R * rA_[k] * N_[k] * N_[k] * rA_[k + 1] +
                                       (double)l * rA_[k] * r * N_[k] * R);
     if (prof_) prof_->begin();
     if (fwd) {
       out = DTensor({L, rA_[k + 1], R}, s_);
-      phi_fwd_A(pd, phi_in.data(), left, Acore(k), right, out.data(), wphi_.p, s_);
+      phi_fwd_A(pd, phi_in.data(), left, Acore(k), right, out.data(), wphi_.p, s_, &spA_[k]);
     } else {
       out = DTensor({l, rA_[k], r}, s_);
-      phi_bck_A(pd, phi_in.data(), left, Acore(k), right, out.data(), wphi_.p, s_);
+      phi_bck_A(pd, phi_in.data(), left, Acore(k), right, out.data(), wphi_.p, s_, &spA_[k]);
     }
     if (prof_) prof_->end(f, 3);
     st_.phi_flops += f;
@@ -272,18 +277,23 @@ class AmenRun {
 
 void AmenRun::init(const TTView& x0, const TTView& z0) {
   const int d = d_;
+  spA_.resize(d);
+  if (p_.a_structure)
+    for (int i = 0; i < d; ++i) spA_[i].build(Acore(i), rA_[i], N_[i], N_[i], rA_[i + 1], s_);
   mixed_ = p_.precision == 1;
   if (mixed_) {
     use_tc_ = (p_.lowp_engine == 2) || (p_.lowp_engine == 0 && tc_available());
     TTGB_REQUIRE(!use_tc_ || tc_available(), "tcgen05 engine needs an sm_100-family GPU");
     if (use_tc_) {
       tc_cores_.resize(d);
-      for (int i = 0; i < d; ++i) tc_cores_[i].build(Acore(i), rA_[i], N_[i], N_[i], rA_[i + 1], s_);
+      for (int i = 0; i < d; ++i)
+        if (!spA_[i].use) tc_cores_[i].build(Acore(i), rA_[i], N_[i], N_[i], rA_[i + 1], s_);
       TTGB_CUDA(cudaMallocAsync((void**)&tc_err_, sizeof(int), s_));
       TTGB_CUDA(cudaMemsetAsync(tc_err_, 0, sizeof(int), s_));
     } else {
       A32_.resize(d);
       for (int i = 0; i < d; ++i) {
+        if (spA_[i].use) continue;   // the FP32 values live in the sparse structure
         const int64_t ne = rA_[i] * N_[i] * N_[i] * rA_[i + 1];
         A32_[i].reset((size_t)ne, s_);
         cast(Acore(i), A32_[i].p, ne, s_);
@@ -509,6 +519,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
     op.dims = LocalOpDims{rk, rA_[k], rk, n, n, rA_[k + 1], rk1, rk1};
     op.phi_l = Phis_[k].data();
     op.A = Acore(k);
+    op.spA = &spA_[k];
     op.phi_r = Phis_[k + 1].data();
     op.prec = p_.prec;
     w1_.ensure(local_product_w1(op.dims), s_);
@@ -709,12 +720,12 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
 void AmenRun::setup_lowp(LocalOperator& op, int k) {
   const LocalOpDims& d = op.dims;
   if (use_tc_) {
-    tc_local_.setup(d, Phis_[k].data(), Phis_[k + 1].data(), &tc_cores_[k], tc_err_, s_);
+    tc_local_.setup(d, Phis_[k].data(), Phis_[k + 1].data(), &tc_cores_[k], &spA_[k], tc_err_,
+                    s_);
     op.lowp = true;
     op.tc = &tc_local_;
     lowp_count_ = 0;
     op.count_lowp = &lowp_count_;
-  op.prof_lowp = prof_lowp_.get();
     op.prof_lowp = prof_lowp_.get();
     return;
   }
@@ -855,6 +866,7 @@ AmenResult AmenRun::run(const TTView& x0, const TTView& z0) {
     prof_lowp_->flush();
     st_.lowp_ms = prof_lowp_->ms;
     st_.lowp_launches = prof_lowp_->launches;
+    st_.lowp_gemm_flops = prof_lowp_->flops;
   }
   res.stats = st_;
   return res;

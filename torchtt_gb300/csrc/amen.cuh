@@ -28,6 +28,7 @@ struct AmenParams {
   int max_refine = 4;          // refinement steps per local solve (mixed)
   int lowp_engine = 0;         // mixed: 0 auto (tcgen05 when available), 1 FP32 CUDA cores, 2 tcgen05
   double lowp_floor = 1e-5;    // relative target of one low-precision inner solve (mixed)
+  int a_structure = 1;         // 1: apply A cores of density < 1/4 from their nonzeros
 };
 
 // A TT-matrix or TT-vector given by device pointers (borrowed).
@@ -61,7 +62,9 @@ struct AmenStats {
   // profile only: CUDA-event time of the low-precision local products (mixed path)
   double lowp_ms = 0.0;
   int64_t lowp_launches = 0;
-  // filled when AmenParams::profile is set: CUDA-event time of the contraction launches
+  double lowp_gemm_flops = 0.0;   // flops of their GEMM launches
+  // filled when AmenParams::profile is set: CUDA-event time of the contraction launches and the
+  // flops of their GEMMs (an A stage run from the nonzeros of a sparse core is not counted)
   double contract_ms = 0.0;
   int64_t contract_launches = 0;
   double contract_flops = 0.0;

@@ -105,6 +105,31 @@ struct Scratch {   // per-call workspace of the kernel-level entry points
 
 namespace ttgb {
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+AmenParams params_from_c(const ttgb_amen_params* params) {
+  TTGB_REQUIRE(params != nullptr, "null parameters");
+  AmenParams p;
+  p.nswp = params->nswp;
+  p.eps = params->eps;
+  p.rmax = params->rmax;
+  p.max_full = params->max_full;
+  p.kickrank = params->kickrank;
+  p.kick2 = params->kick2;
+  p.local_iterations = params->local_iterations;
+  p.resets = params->resets;
+  p.verbose = params->verbose;
+  p.prec = params->preconditioner;
+  p.seed = params->seed;
+  p.profile = params->profile;
+  TTGB_REQUIRE(params->precision == TTGB_PRECISION_FP64 || params->precision == TTGB_PRECISION_MIXED,
+               "invalid precision mode");
+  p.precision = params->precision;
+  TTGB_REQUIRE(params->lowp_engine >= 0 && params->lowp_engine <= 2, "invalid low-precision engine");
+  p.lowp_engine = params->lowp_engine;
+  TTGB_REQUIRE(params->a_structure == 0 || params->a_structure == 1, "invalid a_structure");
+  p.a_structure = params->a_structure;
+  return p;
+}
 }  // namespace ttgb
 
 extern "C" {
@@ -125,6 +150,7 @@ void ttgb_default_params(ttgb_amen_params* p) {
   p->profile = 0;
   p->precision = TTGB_PRECISION_FP64;
   p->lowp_engine = 0;
+  p->a_structure = 1;
 }
 
 int ttgb_amen_solve(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, const ttgb_tt* z0,
@@ -133,24 +159,7 @@ int ttgb_amen_solve(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, const
     TTGB_REQUIRE(A && b && params && out, "A, b, params and out must not be NULL");
     TTView Av = view_of(A, true), bv = view_of(b, false);
     TTView xv = view_of(x0, false), zv = view_of(z0, false);
-    AmenParams p;
-    p.nswp = params->nswp;
-    p.eps = params->eps;
-    p.rmax = params->rmax;
-    p.max_full = params->max_full;
-    p.kickrank = params->kickrank;
-    p.kick2 = params->kick2;
-    p.local_iterations = params->local_iterations;
-    p.resets = params->resets;
-    p.verbose = params->verbose;
-    p.prec = params->preconditioner;
-    p.seed = params->seed;
-    p.profile = params->profile;
-    TTGB_REQUIRE(params->precision == TTGB_PRECISION_FP64 || params->precision == TTGB_PRECISION_MIXED,
-                 "invalid precision mode");
-    p.precision = params->precision;
-    TTGB_REQUIRE(params->lowp_engine >= 0 && params->lowp_engine <= 2, "invalid low-precision engine");
-    p.lowp_engine = params->lowp_engine;
+    const AmenParams p = params_from_c(params);
     auto* sol = new ttgb_solution;
     try {
       sol->res = amen_solve(Av, bv, xv, zv, p, as_stream(stream));
@@ -195,6 +204,7 @@ int ttgb_solution_stats(const ttgb_solution* sol, ttgb_stats* st) {
     for (int i = 0; i < 12; ++i) st->phase_ms[i] = a.phase_ms[i];
     st->lowp_ms = a.lowp_ms;
     st->lowp_launches = a.lowp_launches;
+    st->lowp_gemm_flops = a.lowp_gemm_flops;
   });
 }
 
@@ -264,9 +274,11 @@ int ttgb_local_product(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, i
     cudaStream_t st = as_stream(stream);
     LocalOpDims d{rl, s, r, m, n, S, RL, R};
     DBuf w1(local_product_w1(d), st), w2(local_product_w2(d), st);
+    SparseCore sp;   // the solver's structured A stage when A is sparse enough
+    sp.build(A, s, m, n, S, st);
     for (int32_t i = 0; i < nrhs; ++i)
       local_product(d, phi_l, A, phi_r, x + (int64_t)i * r * n * R, y + (int64_t)i * rl * m * RL,
-                    w1.p, w2.p, st);
+                    w1.p, w2.p, st, 1.0, 0.0, &sp);
   });
 }
 
@@ -287,10 +299,12 @@ int ttgb_local_product_lowp(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t
       TTGB_CUDA(cudaMallocAsync((void**)&err, sizeof(int), st));
       TTGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
       {
+        SparseCore sp;
+        sp.build(A, s, m, n, S, st);
         TcCore core;
-        core.build(A, s, m, n, S, st);
+        if (!sp.use) core.build(A, s, m, n, S, st);
         TcLocal tl;
-        tl.setup(d, phi_l, phi_r, &core, err, st);
+        tl.setup(d, phi_l, phi_r, &core, &sp, err, st);
         tl.apply(x, y, st);
         int herr = 0;
         TTGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -306,7 +320,9 @@ int ttgb_local_product_lowp(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t
       cast(A, a32.p, s * m * n * S, st);
       cast(phi_r, pr.p, RL * S * R, st);
       cast(x, xf.p, (int64_t)nx, st);
-      local_product(d, pl.p, a32.p, pr.p, xf.p, yf.p, w1.p, w2.p, st);
+      SparseCore sp;
+      sp.build(A, s, m, n, S, st);
+      local_product(d, pl.p, a32.p, pr.p, xf.p, yf.p, w1.p, w2.p, st, 1.0f, 0.0f, &sp);
       cast(yf.p, y, (int64_t)ny, st);
     }
   });
@@ -322,8 +338,10 @@ static int phi_A_entry(bool fwd, int64_t l, int64_t L, int64_t s, int64_t S, int
     cudaStream_t st = as_stream(stream);
     PhiDims d{l, L, s, S, r, R, M, N};
     DBuf w(phi_A_workspace(d), st);
-    if (fwd) phi_fwd_A(d, phi, left, A, right, out, w.p, st);
-    else phi_bck_A(d, phi, left, A, right, out, w.p, st);
+    SparseCore sp;
+    sp.build(A, s, M, N, S, st);
+    if (fwd) phi_fwd_A(d, phi, left, A, right, out, w.p, st, &sp);
+    else phi_bck_A(d, phi, left, A, right, out, w.p, st, &sp);
   });
 }
 

@@ -38,6 +38,7 @@ struct KParams {
   AxD cm, cn;
   int64_t c_bs;
   T alpha, beta;
+  int tri;
 };
 
 constexpr int BK = 16;
@@ -54,8 +55,10 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams<T> p) {
   const int bidx = bz / p.splitk;
   const int ks = bz - bidx * p.splitk;
   const int kbeg = ks * p.kchunk;
-  const int kend = min(p.K, kbeg + p.kchunk);
+  int kend = min(p.K, kbeg + p.kchunk);
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  if ((p.tri & kTriLowerC) && m0 + BM <= n0) return;   // tile strictly above the diagonal
+  if (p.tri & kTriUpperB) kend = min(kend, n0 + BN);   // B(k, n) = 0 for k > n
 
   const T* A = p.A + (int64_t)bidx * p.a_bs;
   const T* B = p.B + (int64_t)bidx * p.b_bs;
@@ -175,6 +178,7 @@ void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool determ
   p.B = d.B; p.bk = to_dev(d.bk, d.K); p.bn = to_dev(d.bn, d.N); p.b_bs = d.b_bs;
   p.C = d.C; p.cm = to_dev(d.cm, d.M); p.cn = to_dev(d.cn, d.N); p.c_bs = d.c_bs;
   p.alpha = d.alpha; p.beta = d.beta;
+  p.tri = d.tri;
   if (d.K <= 0) {  // empty sum: C = beta * C
     scale_output_kernel<<<cdiv((int64_t)d.M * d.N * d.batch, 256) > 4096 ? 4096 : cdiv((int64_t)d.M * d.N * d.batch, 256), 256, 0, stream>>>(
         p.C, p.M, p.N, p.batch, p.cm, p.cn, p.c_bs, p.beta);
@@ -236,7 +240,8 @@ void contract(const ContractDescF& d, cudaStream_t stream, bool deterministic) {
 
 template <typename T>
 static void local_product_t(const LocalOpDims& d, const T* phi_l, const T* A, const T* phi_r,
-                            const T* x, T* y, T* w1, T* w2, cudaStream_t stream, T alpha, T beta) {
+                            const T* x, T* y, T* w1, T* w2, cudaStream_t stream, T alpha, T beta,
+                            const SparseCore* sp) {
   // step 1: W[(l,s),(n,R)] = sum_r Phi_l[(l,s), r] X[r, (n,R)]
   {
     ContractDescT<T> c;
@@ -247,7 +252,11 @@ static void local_product_t(const LocalOpDims& d, const T* phi_l, const T* A, co
     contract(c, stream);
   }
   // step 2 (batched over l): Y2_l[(m,S), R] = sum_{(s,n)} A[s,m,n,S] W_l[(s,n), R]
-  {
+  if (sp && sp->use) {
+    // from the nonzeros: Y2[l,(m,S),R] = sum A[s,m,n,S] W[l,s,n,R]
+    const StageDims g{d.rl, d.R, d.s * d.n * d.R, d.m * d.S * d.R, d.R, d.n * d.R, d.R};
+    sparse_stage(sp->lp, w1, w2, g, stream);
+  } else {
     ContractDescT<T> c;
     c.M = (int)(d.m * d.S); c.N = (int)d.R; c.K = (int)(d.s * d.n); c.batch = (int)d.rl;
     c.A = A; c.am = Ax::two(d.S, d.n * d.S, 1); c.ak = Ax::two(d.n, d.m * d.n * d.S, d.S);
@@ -269,14 +278,14 @@ static void local_product_t(const LocalOpDims& d, const T* phi_l, const T* A, co
 
 void local_product(const LocalOpDims& d, const double* phi_l, const double* A, const double* phi_r,
                    const double* x, double* y, double* w1, double* w2, cudaStream_t stream,
-                   double alpha, double beta) {
-  local_product_t<double>(d, phi_l, A, phi_r, x, y, w1, w2, stream, alpha, beta);
+                   double alpha, double beta, const SparseCore* sp) {
+  local_product_t<double>(d, phi_l, A, phi_r, x, y, w1, w2, stream, alpha, beta, sp);
 }
 
 void local_product(const LocalOpDims& d, const float* phi_l, const float* A, const float* phi_r,
                    const float* x, float* y, float* w1, float* w2, cudaStream_t stream,
-                   float alpha, float beta) {
-  local_product_t<float>(d, phi_l, A, phi_r, x, y, w1, w2, stream, alpha, beta);
+                   float alpha, float beta, const SparseCore* sp) {
+  local_product_t<float>(d, phi_l, A, phi_r, x, y, w1, w2, stream, alpha, beta, sp);
 }
 
 size_t phi_A_workspace(const PhiDims& d) {
@@ -286,7 +295,8 @@ size_t phi_A_workspace(const PhiDims& d) {
 }
 
 void phi_fwd_A(const PhiDims& d, const double* phi, const double* left, const double* A,
-               const double* right, double* out, double* work, cudaStream_t stream) {
+               const double* right, double* out, double* work, cudaStream_t stream,
+               const SparseCore* sp) {
   double* T1 = work;                              // [s, r, M, L]
   double* T2 = work + d.s * d.r * d.M * d.L;      // [r, L, N, S]
   {  // T1[(s,r),(M,L)] = sum_l Phi[l,(s,r)] left[l,(M,L)]
@@ -296,6 +306,19 @@ void phi_fwd_A(const PhiDims& d, const double* phi, const double* left, const do
     c.B = left; c.bk = Ax::one(d.M * d.L); c.bn = Ax::one(1);
     c.C = T1; c.cm = Ax::one(d.M * d.L); c.cn = Ax::one(1);
     contract(c, stream);
+  }
+  if (sp && sp->use) {
+    // from the nonzeros, into the key-major layout T2'[N,S,r,L]
+    const StageDims g{d.r, d.L, d.M * d.L, d.L, d.r * d.L, d.r * d.M * d.L, d.L};
+    sparse_stage(sp->fw, T1, T2, g, stream);
+    // out[L,S,R] = sum_{(r,N)} T2'[N,S,r,L] right[r,N,R]   (batched over S)
+    ContractDesc c;
+    c.M = (int)d.L; c.N = (int)d.R; c.K = (int)(d.r * d.N); c.batch = (int)d.S;
+    c.A = T2; c.am = Ax::one(1); c.ak = Ax::two(d.N, d.L, d.S * d.r * d.L); c.a_bs = d.r * d.L;
+    c.B = right; c.bk = Ax::one(d.R); c.bn = Ax::one(1);
+    c.C = out; c.cm = Ax::one(d.S * d.R); c.cn = Ax::one(1); c.c_bs = d.R;
+    contract(c, stream);
+    return;
   }
   {  // T2[(r,L),(N,S)] = sum_{(s,M)} T1[s,r,M,L] A[s,M,N,S]
     ContractDesc c;
@@ -316,7 +339,8 @@ void phi_fwd_A(const PhiDims& d, const double* phi, const double* left, const do
 }
 
 void phi_bck_A(const PhiDims& d, const double* phi, const double* left, const double* A,
-               const double* right, double* out, double* work, cudaStream_t stream) {
+               const double* right, double* out, double* work, cudaStream_t stream,
+               const SparseCore* sp) {
   double* T1 = work;                              // [l, M, S, R]
   double* T2 = work + d.l * d.M * d.S * d.R;      // [l, s, N, R]
   {  // T1[(l,M),(S,R)] = sum_L left[(l,M), L] Phi[L,(S,R)]
@@ -327,7 +351,10 @@ void phi_bck_A(const PhiDims& d, const double* phi, const double* left, const do
     c.C = T1; c.cm = Ax::one(d.S * d.R); c.cn = Ax::one(1);
     contract(c, stream);
   }
-  {  // T2[l,s,N,R] = sum_{(M,S)} T1[l,M,S,R] A[s,M,N,S]; rows (l,R), cols (s,N)
+  if (sp && sp->use) {   // from the nonzeros: key (s,N), free (l, R)
+    const StageDims g{d.l, d.R, d.M * d.S * d.R, d.s * d.N * d.R, d.R, d.S * d.R, d.R};
+    sparse_stage(sp->bk, T1, T2, g, stream);
+  } else {  // T2[l,s,N,R] = sum_{(M,S)} T1[l,M,S,R] A[s,M,N,S]; rows (l,R), cols (s,N)
     ContractDesc c;
     c.M = (int)(d.l * d.R); c.N = (int)(d.s * d.N); c.K = (int)(d.M * d.S);
     c.A = T1; c.am = Ax::two(d.R, d.M * d.S * d.R, 1); c.ak = Ax::two(d.S, d.S * d.R, d.R);

@@ -4,6 +4,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "sparse_a.cuh"
 
 namespace ttgb {
 
@@ -31,7 +32,13 @@ struct ContractDescT {
   Ax cm, cn;
   int64_t c_bs = 0;
   T alpha = T(1), beta = T(0);
+  // structure flags: kTriLowerC computes only output tiles that touch m >= n (a symmetric
+  // product whose upper part is not read); kTriUpperB treats B(k, n) as zero for k > n (an upper
+  // triangular right factor), so a column tile sums only k < its last column.
+  int tri = 0;
 };
+constexpr int kTriLowerC = 1;
+constexpr int kTriUpperB = 2;
 using ContractDesc = ContractDescT<double>;
 using ContractDescF = ContractDescT<float>;
 
@@ -50,12 +57,13 @@ struct LocalOpDims {
   int64_t m, n, S;       // A core: s x m x n x S
   int64_t RL, R;         // Phi_right: RL x S x R
 };
+// `sp` (optional): the nonzero structure of A; when sp->use the A stage runs from it.
 void local_product(const LocalOpDims& d, const double* phi_l, const double* A, const double* phi_r,
                    const double* x, double* y, double* w1, double* w2, cudaStream_t stream,
-                   double alpha = 1.0, double beta = 0.0);
+                   double alpha = 1.0, double beta = 0.0, const SparseCore* sp = nullptr);
 void local_product(const LocalOpDims& d, const float* phi_l, const float* A, const float* phi_r,
                    const float* x, float* y, float* w1, float* w2, cudaStream_t stream,
-                   float alpha = 1.0f, float beta = 0.0f);
+                   float alpha = 1.0f, float beta = 0.0f, const SparseCore* sp = nullptr);
 inline size_t local_product_w1(const LocalOpDims& d) { return size_t(d.rl * d.s * d.n * d.R); }
 inline size_t local_product_w2(const LocalOpDims& d) { return size_t(d.rl * d.m * d.S * d.R); }
 
@@ -72,9 +80,11 @@ struct PhiDims {
 };
 size_t phi_A_workspace(const PhiDims& d);   // doubles needed by phi_fwd_A / phi_bck_A
 void phi_fwd_A(const PhiDims& d, const double* phi, const double* left, const double* A,
-               const double* right, double* out, double* work, cudaStream_t stream);
+               const double* right, double* out, double* work, cudaStream_t stream,
+               const SparseCore* sp = nullptr);
 void phi_bck_A(const PhiDims& d, const double* phi, const double* left, const double* A,
-               const double* right, double* out, double* work, cudaStream_t stream);
+               const double* right, double* out, double* work, cudaStream_t stream,
+               const SparseCore* sp = nullptr);
 struct PhiRhsDims {
   int64_t b, B;   // rhs core ranks (b x n x B)
   int64_t r, R;   // solution core ranks (r x n x R)

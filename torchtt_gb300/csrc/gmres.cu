@@ -19,23 +19,23 @@ void LocalOperator::apply(const double* x, double* y, bool use_prec, cudaStream_
       tc->apply(in, y, s);
     } else {
       cast(in, xf, size(), s);
-      local_product(dims, phi_l32, A32, phi_r32, xf, yf, w1f, w2f, s);
+      local_product(dims, phi_l32, A32, phi_r32, xf, yf, w1f, w2f, s, 1.0f, 0.0f, spA);
       cast(yf, y, dims.rl * dims.m * dims.RL, s);
     }
-    if (prof_lowp) prof_lowp->end(local_product_flops(dims), tc ? 4 : 5);
+    if (prof_lowp) prof_lowp->end(local_product_gemm_flops(dims, spA), tc ? 4 : 5);
     if (count_lowp) ++*count_lowp;
     return;
   }
   if (prof) prof->begin();
-  local_product(dims, phi_l, A, phi_r, in, y, w1, w2, s);
-  if (prof) prof->end(local_product_flops(dims), 3);
+  local_product(dims, phi_l, A, phi_r, in, y, w1, w2, s, 1.0, 0.0, spA);
+  if (prof) prof->end(local_product_gemm_flops(dims, spA), 3);
   if (count) ++*count;
 }
 
 void LocalOperator::apply_fp64(const double* x, double* y, cudaStream_t s) const {
   if (prof) prof->begin();
-  local_product(dims, phi_l, A, phi_r, x, y, w1, w2, s);
-  if (prof) prof->end(local_product_flops(dims), 3);
+  local_product(dims, phi_l, A, phi_r, x, y, w1, w2, s, 1.0, 0.0, spA);
+  if (prof) prof->end(local_product_gemm_flops(dims, spA), 3);
   if (count) ++*count;
 }
 

@@ -15,6 +15,14 @@ inline double local_product_flops(const LocalOpDims& d) {
          2.0 * d.rl * d.m * (double)d.RL * d.S * d.R;
 }
 
+// flops executed by the GEMM launches of one local product: the A stage is excluded when it runs
+// from the nonzeros of a sparse core (it is then a gather, bounded by memory, not by flops)
+inline double local_product_gemm_flops(const LocalOpDims& d, const SparseCore* sp) {
+  if (sp && sp->use)
+    return 2.0 * d.rl * d.n * d.R * (double)d.s * d.r + 2.0 * d.rl * d.m * (double)d.RL * d.S * d.R;
+  return local_product_flops(d);
+}
+
 enum Prec : int { kNoPrec = 0, kCPrec = 1, kRPrec = 2 };   // cpp/define.h:10-12
 
 // y = B x with B = Phi_left x A_k x Phi_right (the projected operator), optionally composed with
@@ -24,6 +32,7 @@ struct LocalOperator {
   const double* phi_l = nullptr;
   const double* A = nullptr;
   const double* phi_r = nullptr;
+  const SparseCore* spA = nullptr;   // nonzero structure of A (structured A stage), optional
   int prec = kNoPrec;
   const double* J = nullptr;    // preconditioner blocks (see prec.cu)
   double* w1 = nullptr;         // local_product workspaces

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(512) chol_kernel(double* G, int n, int64_t shi
     double mx = 0.0;
     for (int64_t t = tid; t < (int64_t)n * n; t += nt) {
       const int i = (int)(t / n), k = (int)(t % n);
+      if (k < i) continue;   // the Gram matrix is formed (and read) in its upper triangle only
       const double v = G[t] - (i == k ? 1.0 : 0.0);
       mx = fmax(mx, isfinite(v) ? fabs(v) : 1e300);
     }
@@ -131,6 +132,7 @@ __global__ void __launch_bounds__(512) chol_inv_smem_kernel(const double* __rest
     double mx = 0.0;
     for (int t = tid; t < n * n; t += nt) {
       const int i = t / n, k = t % n;
+      if (k < i) continue;   // the Gram matrix is formed (and read) in its upper triangle only
       const double v = G[i * ld + k] - (i == k ? 1.0 : 0.0);
       mx = fmax(mx, isfinite(v) ? fabs(v) : 1e300);
     }
@@ -657,7 +659,7 @@ void householder(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, 
 
 void gemm_cm(const double* A, int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
              int64_t m, int64_t n, int64_t k, double alpha, double beta, cudaStream_t s,
-             bool transA, bool transB) {
+             bool transA, bool transB, int tri) {
   ContractDesc c;
   c.M = (int)m; c.N = (int)n; c.K = (int)k;
   c.A = A;
@@ -668,6 +670,7 @@ void gemm_cm(const double* A, int64_t lda, const double* B, int64_t ldb, double*
   else { c.bk = Ax::one(ldb); c.bn = Ax::one(1); }
   c.C = C; c.cm = Ax::one(1); c.cn = Ax::one(ldc);
   c.alpha = alpha; c.beta = beta;
+  c.tri = tri;
   contract(c, s);
 }
 
@@ -696,7 +699,8 @@ QRResult qr(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, doubl
   int64_t ldin = lda;
   double* outs[3] = {Q, Qt, Q};
   for (int pass = 0; pass < 3; ++pass) {
-    gemm_cm(Ain, ldin, Ain, ldin, G, n, n, n, m, 1.0, 0.0, s, true, false);
+    // Gram matrix: only its lower (column-major) = upper (row-major) triangle is formed and read
+    gemm_cm(Ain, ldin, Ain, ldin, G, n, n, n, m, 1.0, 0.0, s, true, false, kTriLowerC);
     if (n <= kCholSmemMax) {
       const size_t smem = (size_t)2 * n * (n + 1) * sizeof(double);
       smem_optin((const void*)chol_inv_smem_kernel,
@@ -710,8 +714,8 @@ QRResult qr(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, doubl
       trinv_kernel<<<cdiv(n, 128), 128, 0, s>>>(G, Ri, (int)n);
       TTGB_CHECK_LAUNCH();
     }
-    // Q_next = Ain * R^{-1}   (Ri row-major == (Ri)^T column-major)
-    gemm_cm(Ain, ldin, Ri, n, outs[pass], m, m, n, n, 1.0, 0.0, s, false, true);
+    // Q_next = Ain * R^{-1}   (Ri row-major == (Ri)^T column-major; R^{-1} upper triangular)
+    gemm_cm(Ain, ldin, Ri, n, outs[pass], m, m, n, n, 1.0, 0.0, s, false, true, kTriUpperB);
     if (pass == 0) {
       copy(G, Rt, n * n, s);
     } else {  // Rt <- R_pass * Rt  (row-major products via column-major transposes)

@@ -40,9 +40,10 @@ void lu_solve(const double* B, int64_t n, const double* rhs, double* x, LinalgWS
 // y = B x for the n x n row-major B
 void gemv(const double* B, int64_t n, const double* x, double* y, cudaStream_t s);
 
-// C (m x n col-major, ldc) = A (m x k col-major, lda) * B (k x n col-major, ldb)  [FP64]
+// C (m x n col-major, ldc) = A (m x k col-major, lda) * B (k x n col-major, ldb)  [FP64];
+// `tri`: structure flags of the contraction engine (kTriLowerC, kTriUpperB)
 void gemm_cm(const double* A, int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
              int64_t m, int64_t n, int64_t k, double alpha, double beta, cudaStream_t s,
-             bool transA = false, bool transB = false);
+             bool transA = false, bool transB = false, int tri = 0);
 
 }  // namespace ttgb

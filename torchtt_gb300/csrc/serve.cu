@@ -180,12 +180,8 @@ int ttgb_server_submit(ttgb_server* srv, const ttgb_tt* A, const ttgb_tt* b, con
     req->b = copy_view(b, false);
     req->x0 = copy_view(x0, false);
     TTGB_REQUIRE(req->A.d >= 1 && req->A.d == req->b.d, "Dimension mismatch.");
-    AmenParams& p = req->p;
-    p.nswp = params->nswp; p.eps = params->eps; p.rmax = params->rmax; p.max_full = params->max_full;
-    p.kickrank = params->kickrank; p.kick2 = params->kick2;
-    p.local_iterations = params->local_iterations; p.resets = params->resets;
-    p.verbose = params->verbose; p.prec = params->preconditioner; p.seed = params->seed;
-    p.profile = params->profile; p.precision = params->precision; p.lowp_engine = params->lowp_engine;
+    req->p = params_from_c(params);
+    const AmenParams& p = req->p;
     req->footprint = estimate_footprint(req->A, req->b, p);
     std::lock_guard<std::mutex> lock(srv->mu);
     TTGB_REQUIRE(!srv->stopping, "server is shutting down");

@@ -6,3 +6,9 @@
 struct ttgb_solution {
   ttgb::AmenResult res;
 };
+
+struct ttgb_amen_params;
+namespace ttgb {
+// Validated copy of the C parameter block (throws kInvalidArgument on bad values).
+AmenParams params_from_c(const ttgb_amen_params* params);
+}  // namespace ttgb

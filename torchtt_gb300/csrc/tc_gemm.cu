@@ -53,12 +53,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   return false;
 }
 
-__device__ __forceinline__ float to_tf32(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-
 __device__ __forceinline__ int64_t tc_off(const TcAx& a, int i) {
   const int i1 = i / a.e0;
   const int i0 = i - i1 * a.e0;

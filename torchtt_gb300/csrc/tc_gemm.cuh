@@ -53,4 +53,11 @@ void split_tf32(const double* x, const Gather4& g, float* hi, float* lo, cudaStr
 // true when the device supports tcgen05 (sm_100 family)
 bool tc_available();
 
+// round an FP32 value to TF32 (round to nearest, ties away), as the tensor core reads it
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
 }  // namespace ttgb

@@ -16,9 +16,10 @@ void TcCore::build(const double* A, int64_t s, int64_t m, int64_t n, int64_t S, 
 }
 
 void TcLocal::setup(const LocalOpDims& dims, const double* phi_l, const double* phi_r,
-                    const TcCore* c, int* errflag, cudaStream_t st) {
+                    const TcCore* c, const SparseCore* spa, int* errflag, cudaStream_t st) {
   d = dims;
   core = c;
+  sp = (spa && spa->use) ? spa : nullptr;
   err = errflag;
   const size_t nl = (size_t)(d.rl * d.s * d.r), nr = (size_t)(d.RL * d.S * d.R);
   phl_h.ensure(nl, st); phl_l.ensure(nl, st);
@@ -31,7 +32,8 @@ void TcLocal::setup(const LocalOpDims& dims, const double* phi_l, const double* 
   const size_t nx = (size_t)(d.r * d.n * d.R);
   const size_t nw = (size_t)(d.rl * d.R * d.s * d.n), ny = (size_t)(d.rl * d.m * d.S * d.R);
   xh.ensure(nx, st); xl.ensure(nx, st);
-  wh.ensure(nw, st); wl.ensure(nw, st);
+  if (sp) wf.ensure(nw, st);
+  else { wh.ensure(nw, st); wl.ensure(nw, st); }
   yh.ensure(ny, st); yl.ensure(ny, st);
 }
 
@@ -44,6 +46,21 @@ void TcLocal::apply(const double* x, double* y, cudaStream_t st) {
     g.e3 = d.n; g.s3 = d.R;
     split_tf32(x, g, xh.p, xl.p, st);
   }
+  if (sp) {
+    {   // W[l][s][n][R] = x^P[(n,R), r] . Phi_l[(l,s), r]   (FP32)
+      TcGemm t;
+      t.M = (int)(d.n * d.R); t.N = (int)(d.rl * d.s); t.K = (int)d.r;
+      t.A_hi = xh.p; t.A_lo = xl.p; t.lda = d.r;
+      t.B_hi = phl_h.p; t.B_lo = phl_l.p; t.ldb = d.r;
+      t.out = kTcOutF32; t.C32 = wf.p;
+      t.cm.e0 = (int)d.R; t.cm.s0 = 1; t.cm.s1 = d.R;                          // row (n, R)
+      t.cn.e0 = (int)d.s; t.cn.s0 = d.n * d.R; t.cn.s1 = d.s * d.n * d.R;      // col (l, s)
+      tc_gemm(t, err, st);
+    }
+    // Y2[l][(m,S)][R] = sum A[s,m,n,S] W[l][s][n][R], written as the TF32 split
+    const StageDims g{d.rl, d.R, d.s * d.n * d.R, d.m * d.S * d.R, d.R, d.n * d.R, d.R};
+    sparse_stage_split(sp->lp, wf.p, yh.p, yl.p, g, st);
+  } else {
   {   // W[l][R][s][n] = x^P[(n,R), r] . Phi_l[(l,s), r]
     TcGemm t;
     t.M = (int)(d.n * d.R); t.N = (int)(d.rl * d.s); t.K = (int)d.r;
@@ -62,6 +79,7 @@ void TcLocal::apply(const double* x, double* y, cudaStream_t st) {
     t.out = kTcOutSplit; t.C_hi = yh.p; t.C_lo = yl.p;
     t.cm.s0 = d.R; t.cn.s0 = 1; t.c_bs = d.m * d.S * d.R;
     tc_gemm(t, err, st);
+  }
   }
   {   // y[(l,m), L] = Y2[(l,m),(S,R)] . Phi_r[L,(S,R)]
     TcGemm t;

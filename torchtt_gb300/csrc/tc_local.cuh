@@ -5,6 +5,8 @@
 //   Y2[l][m][S][R]  = A'  [(m,S),(s,n)] . W_l  [R, (s,n)]^T        (batched over l; A' = A permuted)
 //   y [l][m][L]     = Y2  [(l,m),(S,R)] . Phi_r [L, (S,R)]^T
 // Each epilogue writes the next operand directly as a TF32 hi/lo split; the last writes FP64.
+// With a sparse A core the middle GEMM is replaced by the structured A stage: W is written in
+// FP32 as W[l][s][n][R] and the stage writes Y2 as the TF32 split.
 #pragma once
 
 #include "contract.cuh"
@@ -21,10 +23,11 @@ struct TcCore {
 struct TcLocal {
   LocalOpDims d{};
   const TcCore* core = nullptr;
-  FBuf phl_h, phl_l, phr_h, phr_l, xh, xl, wh, wl, yh, yl;
+  const SparseCore* sp = nullptr;   // when sp->use, the A stage runs from the nonzeros (FP32)
+  FBuf phl_h, phl_l, phr_h, phr_l, xh, xl, wh, wl, yh, yl, wf;
   int* err = nullptr;   // device flag of the bounded waits
   void setup(const LocalOpDims& dims, const double* phi_l, const double* phi_r, const TcCore* c,
-             int* errflag, cudaStream_t st);
+             const SparseCore* spa, int* errflag, cudaStream_t st);
   void apply(const double* x, double* y, cudaStream_t st);
 };
 

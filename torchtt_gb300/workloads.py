@@ -233,3 +233,40 @@ def small_random_system(seed=0, N=(4, 5, 6), RA=(1, 2, 3, 1), RX=(1, 2, 3, 1)):
         b.append(t.reshape(a.shape[0] * c.shape[0], a.shape[1], a.shape[3] * c.shape[2]))
     return dict(name="random_%s" % "x".join(map(str, N)), A=_to_torch(A), b=_to_torch(b),
                 x=_to_torch(x), x0=None, params=dict(eps=1e-10))
+
+
+def rounding_stress_d16_n32(index, seed=4):
+    """One solve of the 128-solve rounding batch: d=16, n=32, A = Laplacian + C C^T + I (C a random
+    rank-2 TT-matrix with N(0, 0.01^2) cores, so the perturbation has rank 4 and A is SPD); b = the
+    sum of 4 random rank-16 TTs (input rank 64, N(0,1) cores), to be rounded to ``round_b`` before
+    the solve; eps 1e-8."""
+    d, n = 16, 32
+    A = laplace_lowrank_spd_ttm(d, n, seed)
+    parts = [random_tt([n] * d, [1] + [16] * (d - 1) + [1], seed * 100003 + 4 * index + i,
+                       normalise=False) for i in range(4)]
+    return dict(name="rounding_stress_d16_n32", A=A, b=tt_sum(parts), x0=None, round_b=1e-8,
+                params=dict(eps=1e-8, nswp=20, kickrank=8))
+
+
+def serving_request(index, seed=5):
+    """One request of the serving trace: d ~ U{8..24}, n in {16, 32, 64}, rhs rank ~ U{1..32}
+    (N(0,1) cores, ||b|| = 1), operator = anisotropic Laplacian sum_k c_k L_k with c_k ~ U[0.1, 10],
+    eps in {1e-6, 1e-8, 1e-10}; the reference's other defaults."""
+    g = _rng(seed * 1000003 + index)
+    d = int(g.integers(8, 25))
+    n = int(g.choice([16, 32, 64]))
+    r = int(g.integers(1, 33))
+    coeffs = g.uniform(0.1, 10.0, size=d)
+    eps = float(g.choice([1e-6, 1e-8, 1e-10]))
+    A = laplace_ttm(d, n, coeffs=coeffs)
+    b = random_tt([n] * d, [1] + [r] * (d - 1) + [1], seed * 1000003 + index + 11)
+    return dict(name="serving_request", A=A, b=b, x0=None, d=d, n=n, rhs_rank=r,
+                params=dict(eps=eps))
+
+
+def serving_trace(count, rate, seed=5):
+    """Poisson arrivals: ``count`` requests at ``rate`` per second; returns [(t_arrival, index)]
+    with the request of each index given by ``serving_request(index, seed)``."""
+    g = _rng(seed * 7919 + 1)
+    t = np.cumsum(g.exponential(1.0 / rate, size=count))
+    return [(float(t[i]), i) for i in range(count)]
