@@ -122,6 +122,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x, dist, device):
+    """The largest of the ranks' values (timing is reported for the slowest rank)."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_seeds(seed, rank, batch):
+    """Right-hand-side seeds of one rank's batch: disjoint across ranks (weak scaling)."""
+    return [seed + rank * batch + j for j in range(batch)]
+
+
 def percentile(xs, q):
     xs = sorted(xs)
     if not xs:
@@ -209,7 +222,7 @@ def run_gb300(args):
     from torchtt_gb300.solvers import solve_cores
 
     nb = args.batch
-    seeds = [args.seed + rank * nb + j for j in range(nb)]
+    seeds = rank_seeds(args.seed, rank, nb)
     wls = [get_workload(args.workload, s) for s in seeds]
     p = wls[0]["params"]
     kw = dict(nswp=p.get("nswp", 22), eps=p["eps"], kickrank=p["kickrank"])
@@ -256,9 +269,7 @@ def run_gb300(args):
     step_ms = [ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(args.steps)]
     elapsed_ms = sum(step_ms)
     if ws > 1:
-        t = torch.tensor([elapsed_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+        elapsed_ms = max_over_ranks(elapsed_ms, dist, dev)
     value = ws * nb * args.steps / (elapsed_ms / 1000.0)
 
     # ---- the plain FP64 path, one solve at a time (the comparison point) ------------------------
@@ -355,9 +366,7 @@ def run_gb300(args):
         d2h = sum(c.numel() * 8 for x, _ in out for c in x.cores)
     e2e_s = time.perf_counter() - t0
     if ws > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dist, dev)
     e2e_val = ws * nb * e2e_steps / e2e_s
     srv_stats = srv.stats()
     srv.close()

@@ -6,6 +6,7 @@
 // factors (Cholesky, triangular inverse, Jacobi) run inside one thread block.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "contract.cuh"
@@ -293,6 +294,84 @@ __global__ void __launch_bounds__(512) householder_kernel(double* W, int m, int 
 }
 
 // ---------------------------------------------------------------------------------------------
+// Batched R-only Householder QR, one block per matrix: block b factors W + b * stride (rows x n,
+// column-major, ld rows) in place and writes its R factor as the n x n column-major block
+// Rout + b * n * n (upper triangle; rows >= min(rows, n) and the lower part zero). The levels of
+// the TSQR reduction in qr_r are launches of this kernel.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) householder_r_kernel(double* Wall, int64_t stride, int rows,
+                                                            int n, double* Rout) {
+  __shared__ double sh[32];
+  double* W = Wall + (int64_t)blockIdx.x * stride;
+  double* R = Rout + (int64_t)blockIdx.x * n * n;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const int k = min(rows, n);
+  for (int j = 0; j < k; ++j) {
+    double* col = W + (int64_t)j * rows;
+    double xs = 0.0;
+    for (int i = j + 1 + tid; i < rows; i += nt) xs = fma(col[i], col[i], xs);
+    xs = block_sum_d(xs, sh);
+    const double alpha = col[j];
+    const double nrm = sqrt(alpha * alpha + xs);
+    double tj = 0.0, beta = alpha, scale = 0.0;
+    if (xs > 0.0) {
+      beta = -copysign(nrm, alpha);
+      tj = (beta - alpha) / beta;
+      scale = 1.0 / (alpha - beta);
+    }
+    for (int i = j + 1 + tid; i < rows; i += nt) col[i] *= scale;
+    __syncthreads();
+    if (tid == 0) col[j] = beta;
+    __syncthreads();
+    if (tj != 0.0) {
+      for (int c = j + 1 + warp; c < n; c += nw) {
+        double* cc = W + (int64_t)c * rows;
+        const double c0 = cc[j];
+        double w = 0.0;
+        for (int i = j + 1 + lane; i < rows; i += 32) w = fma(col[i], cc[i], w);
+        w = warp_sum_d(w) + c0;
+        const double tw = tj * w;
+        if (lane == 0) cc[j] -= tw;
+        for (int i = j + 1 + lane; i < rows; i += 32) cc[i] = fma(-tw, col[i], cc[i]);
+      }
+    }
+    __syncthreads();
+  }
+  for (int64_t t = tid; t < (int64_t)n * n; t += nt) {
+    const int i = (int)(t % n), c = (int)(t / n);
+    R[t] = (i <= c && i < k) ? W[(int64_t)c * rows + i] : 0.0;
+  }
+}
+
+// Level-0 gather of TSQR: block b = rows [b*mb, b*mb + mb) of A (zero past m), column-major mb x n.
+__global__ void tsqr_gather_kernel(const double* __restrict__ A, int64_t lda, int64_t m, int n,
+                                   int mb, int nblk, double* W) {
+  const int64_t per = (int64_t)mb * n, total = per * nblk;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / per, rem = t - b * per;
+    const int64_t j = rem / mb, i = rem - j * mb;
+    const int64_t row = b * mb + i;
+    W[t] = (row < m) ? A[j * lda + row] : 0.0;
+  }
+}
+
+// Next TSQR level: block b = [R_{2b}; R_{2b+1}] (2n x n column-major; zero when 2b+1 is missing).
+__global__ void tsqr_stack_kernel(const double* __restrict__ R, int n, int nin, double* W) {
+  const int nout = (nin + 1) / 2;
+  const int64_t per = (int64_t)2 * n * n, total = per * nout;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / per, rem = t - b * per;
+    const int64_t j = rem / (2 * n), i = rem - j * 2 * n;
+    const int64_t src = 2 * b + (i >= n ? 1 : 0);
+    const int64_t ii = i >= n ? i - n : i;
+    W[t] = (src < nin) ? R[src * n * n + j * n + ii] : 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
 // One-sided (Hestenes) Jacobi SVD of the n x n column-major matrix W in one thread block, with
 // the round-robin parallel ordering; rotation formulas of Demmel & Veselic (SIAM J. Matrix Anal.
 // Appl. 13, 1992). On exit U (n x n) holds W_j / sigma_j, V the accumulated rotations, both with
@@ -504,6 +583,158 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
   }
 }
 
+// Block variant of the cluster Jacobi for 16 <= n <= kJacobiBlockMaxN: the columns (padded to
+// P = 2C blocks of nb) are treated as P blocks paired by the round-robin tournament; in round r the
+// CTA i holds the blocks rr(i, r) and rr(P-1-i, r) in its own shared memory and rotates all their
+// cross pairs there (nb sub-rounds of nb disjoint pairs, block barrier only; the pairs inside a
+// block are rotated in the first round of each sweep), then pulls the two blocks of its next
+// pair from their holders over DSMEM into its second buffer. Every pair of columns is visited once
+// per sweep, as in the scalar cyclic order, with one cluster barrier per round (P - 1 per sweep)
+// instead of one per pair round (n - 1 per sweep), and every dot product reads local memory.
+constexpr int kJacobiBlockMaxN = 160;
+
+__device__ __forceinline__ int jacobi_rotate_pair(double* wp, double* wq, double* vp, double* vq,
+                                                  int n, double tol, int lane) {
+  double a = 0.0, b = 0.0, g = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const double x = wp[i], y = wq[i];
+    a = fma(x, x, a); b = fma(y, y, b); g = fma(x, y, g);
+  }
+  a = warp_sum_d(a); b = warp_sum_d(b); g = warp_sum_d(g);
+  if (a == 0.0 || b == 0.0) return 0;
+  if (!(fabs(g) > tol * sqrt(a) * sqrt(b))) return 0;
+  const double zeta = (b - a) / (2.0 * g);
+  const double t = (fabs(zeta) > 1e150) ? 0.5 / zeta
+                                         : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+  const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+  for (int i = lane; i < n; i += 32) {
+    const double x = wp[i], y = wq[i];
+    wp[i] = c * x - s * y;
+    wq[i] = s * x + c * y;
+    const double u = vp[i], v = vq[i];
+    vp[i] = c * u - s * v;
+    vq[i] = s * u + c * v;
+  }
+  return 1;
+}
+
+__global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
+    jacobi_block_kernel(const double* __restrict__ Win, int n, double* Wout, double* Vout,
+                        int max_sweeps, int* status) {
+  extern __shared__ double sm[];
+  cg::cluster_group cluster = cg::this_cluster();
+  constexpr int C = kJacobiCluster, P = 2 * kJacobiCluster;
+  const int rank = (int)cluster.block_rank();
+  const int nb = (n + P - 1) / P;
+  const int64_t blk = (int64_t)nb * n;   // doubles of one block of W (or of V)
+  // buffer x (0/1), slot s (0/1): W block then V block
+  auto Wb = [&](double* base, int x, int sl) { return base + ((int64_t)(x * 2 + sl) * 2) * blk; };
+  auto Vb = [&](double* base, int x, int sl) { return base + ((int64_t)(x * 2 + sl) * 2 + 1) * blk; };
+  __shared__ int counts[kJacobiCluster];
+  __shared__ int local_cnt;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const double tol = fmax((double)n, 1.0) * kEps;
+  // round 0 of sweep 0: slot 0 holds block rank, slot 1 block P-1-rank
+  for (int sl = 0; sl < 2; ++sl) {
+    const int b = sl == 0 ? rank : P - 1 - rank;
+    double* W = Wb(sm, 0, sl);
+    double* V = Vb(sm, 0, sl);
+    for (int64_t t = tid; t < blk; t += nt) {
+      const int j = (int)(t / n), i = (int)(t - (int64_t)j * n);
+      const int c = b * nb + j;
+      W[t] = (c < n) ? Win[(int64_t)c * n + i] : 0.0;
+      V[t] = (c < n && i == c) ? 1.0 : 0.0;
+    }
+  }
+  int* counts0 = cluster.map_shared_rank(counts, 0);
+  int x = 0, r = 0, sweep = 0, mine = 0;
+  bool converged = false;
+  if (tid == 0) local_cnt = 0;
+  __syncthreads();
+  while (true) {
+    const int bA = rr_index(rank, r, P), bB = rr_index(P - 1 - rank, r, P);
+    double* WA = Wb(sm, x, 0); double* VA = Vb(sm, x, 0);
+    double* WB = Wb(sm, x, 1); double* VB = Vb(sm, x, 1);
+    if (r == 0) {   // pairs inside each block, once per sweep
+      const int m2 = nb + (nb & 1);
+      for (int t = 0; t < m2 - 1; ++t) {
+        for (int task = warp; task < m2; task += nw) {   // m2/2 pairs per slot, 2 slots
+          const int sl = task / (m2 / 2), pi = task % (m2 / 2);
+          int p = rr_index(pi, t, m2), q = rr_index(m2 - 1 - pi, t, m2);
+          if (p > q) { const int u = p; p = q; q = u; }
+          if (q >= nb) continue;
+          double* W = sl ? WB : WA;
+          double* V = sl ? VB : VA;
+          mine += jacobi_rotate_pair(W + (int64_t)p * n, W + (int64_t)q * n, V + (int64_t)p * n,
+                                     V + (int64_t)q * n, n, tol, lane);
+        }
+        __syncthreads();
+      }
+    }
+    for (int t = 0; t < nb; ++t) {   // cross pairs (j, j + t mod nb)
+      for (int j = warp; j < nb; j += nw) {
+        const int k = (j + t) % nb;
+        const int ga = bA * nb + j, gb = bB * nb + k;
+        double *wp = WA + (int64_t)j * n, *wq = WB + (int64_t)k * n;
+        double *vp = VA + (int64_t)j * n, *vq = VB + (int64_t)k * n;
+        if (ga > gb) { double* u = wp; wp = wq; wq = u; u = vp; vp = vq; vq = u; }
+        mine += jacobi_rotate_pair(wp, wq, vp, vq, n, tol, lane);
+      }
+      __syncthreads();
+    }
+    const bool sweep_end = (r == P - 2);
+    if (sweep_end) {
+      if (lane == 0 && mine) atomicAdd(&local_cnt, mine);
+      mine = 0;
+      __syncthreads();
+      if (tid == 0) { counts0[rank] = local_cnt; local_cnt = 0; }
+    }
+    cluster.sync();   // every CTA finished round r (and published its count at a sweep end)
+    if (sweep_end) {
+      int total = 0;
+      for (int c = 0; c < C; ++c) total += counts0[c];
+      ++sweep;
+      if (total == 0) { converged = true; break; }
+      if (sweep >= max_sweeps) break;
+    }
+    // pull the blocks of round r+1 into buffer 1-x from their holders' buffer x
+    const int rn = (r + 1) % (P - 1);
+    for (int sl = 0; sl < 2; ++sl) {
+      const int b = rr_index(sl == 0 ? rank : P - 1 - rank, rn, P);
+      int owner = 0, oslot = 0;
+      for (int c = 0; c < C; ++c) {
+        if (rr_index(c, r, P) == b) { owner = c; oslot = 0; }
+        if (rr_index(P - 1 - c, r, P) == b) { owner = c; oslot = 1; }
+      }
+      const double* srcW = cluster.map_shared_rank(Wb(sm, x, oslot), owner);
+      const double* srcV = cluster.map_shared_rank(Vb(sm, x, oslot), owner);
+      double* dW = Wb(sm, 1 - x, sl);
+      double* dV = Vb(sm, 1 - x, sl);
+      for (int64_t t = tid; t < blk; t += nt) { dW[t] = srcW[t]; dV[t] = srcV[t]; }
+    }
+    __syncthreads();
+    x = 1 - x;
+    r = rn;
+  }
+  if (rank == 0 && tid == 0 && !converged) *status = 3;
+  // buffer x holds the blocks of round r
+  for (int sl = 0; sl < 2; ++sl) {
+    const int b = rr_index(sl == 0 ? rank : P - 1 - rank, r, P);
+    const double* W = Wb(sm, x, sl);
+    const double* V = Vb(sm, x, sl);
+    for (int64_t t = tid; t < blk; t += nt) {
+      const int j = (int)(t / n), i = (int)(t - (int64_t)j * n);
+      const int c = b * nb + j;
+      if (c < n) {
+        Wout[(int64_t)c * n + i] = W[t];
+        Vout[(int64_t)c * n + i] = V[t];
+      }
+    }
+  }
+  cluster.sync();   // no CTA leaves while another may still read its shared memory
+}
+
 // From the rotated W (column-major n x n) and the rotations V: sigma_j = ||W_j||, descending order;
 // Un[:, rank_j] = W_j / sigma_j, Vs[:, rank_j] = V_j, S[rank_j] = sigma_j. One block.
 __global__ void __launch_bounds__(1024) svd_sort_kernel(const double* __restrict__ W,
@@ -657,6 +888,39 @@ void householder(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, 
 
 }  // namespace
 
+void qr_r(const double* A, int64_t lda, int64_t m, int64_t n, double* R, LinalgWS& ws,
+          cudaStream_t s) {
+  if (m <= 0 || n <= 0) return;
+  TTGB_REQUIRE(n <= 4096, "qr_r: too many columns");
+  const int mb = (int)std::max<int64_t>(2 * n, 256);
+  const int64_t nblk = (m + mb - 1) / mb;
+  TTGB_REQUIRE(nblk < 65536, "qr_r: too many row blocks");
+  const int64_t per0 = (int64_t)mb * n;
+  ws.d.ensure((size_t)(per0 * nblk + 2 * n * n * ((nblk + 1) / 2) + 16), s);
+  ws.e.ensure((size_t)(n * n * nblk + 16), s);
+  double* W = ws.d.p;
+  double* Rb = ws.e.p;
+  unsigned g = cdiv(per0 * nblk, 256);
+  if (g > 8192) g = 8192;
+  tsqr_gather_kernel<<<g, 256, 0, s>>>(A, lda, m, (int)n, mb, (int)nblk, W);
+  TTGB_CHECK_LAUNCH();
+  householder_r_kernel<<<(unsigned)nblk, 512, 0, s>>>(W, per0, mb, (int)n, Rb);
+  TTGB_CHECK_LAUNCH();
+  int64_t cur = nblk;
+  while (cur > 1) {
+    const int64_t nxt = (cur + 1) / 2;
+    const int64_t per = 2 * n * n;
+    unsigned g2 = cdiv(per * nxt, 256);
+    if (g2 > 8192) g2 = 8192;
+    tsqr_stack_kernel<<<g2, 256, 0, s>>>(Rb, (int)n, (int)cur, W);
+    TTGB_CHECK_LAUNCH();
+    householder_r_kernel<<<(unsigned)nxt, 512, 0, s>>>(W, per, (int)(2 * n), (int)n, Rb);
+    TTGB_CHECK_LAUNCH();
+    cur = nxt;
+  }
+  copy(Rb, R, n * n, s);
+}
+
 void gemm_cm(const double* A, int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
              int64_t m, int64_t n, int64_t k, double alpha, double beta, cudaStream_t s,
              bool transA, bool transB, int tri) {
@@ -763,10 +1027,17 @@ void svd(const double* A, int64_t lda, int64_t m, int64_t n, double* U, double* 
   transpose(Rb.p, n, W, n, n, n, s);
   DBuf Up((size_t)(n * n), s);   // U' (normalised columns of the rotated R^T, sorted)
   if (n <= kJacobiClusterMaxN && n >= 2 * kJacobiCluster) {
-    const int ncl = (int)((n + kJacobiCluster - 1) / kJacobiCluster);
-    const size_t smem = (size_t)2 * ncl * n * sizeof(double);
-    smem_optin((const void*)jacobi_cluster_kernel, (int)smem);
-    jacobi_cluster_kernel<<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status);
+    if (n <= kJacobiBlockMaxN) {
+      const int nb = (int)((n + 2 * kJacobiCluster - 1) / (2 * kJacobiCluster));
+      const size_t smem = (size_t)8 * nb * n * sizeof(double);
+      smem_optin((const void*)jacobi_block_kernel, (int)smem);
+      jacobi_block_kernel<<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status);
+    } else {
+      const int ncl = (int)((n + kJacobiCluster - 1) / kJacobiCluster);
+      const size_t smem = (size_t)2 * ncl * n * sizeof(double);
+      smem_optin((const void*)jacobi_cluster_kernel, (int)smem);
+      jacobi_cluster_kernel<<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status);
+    }
     TTGB_CHECK_LAUNCH();
     DBuf sig((size_t)n, s);
     svd_sort_kernel<<<1, 1024, 0, s>>>(W, Vw, (int)n, Up.p, S, Vw + n * n, sig.p);

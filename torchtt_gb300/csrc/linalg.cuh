@@ -26,6 +26,12 @@ struct QRResult {
 QRResult qr(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, double* R,
             LinalgWS& ws, const RedWS& red, cudaStream_t s);
 
+// R factor only (n x n column-major, ld n; rows past min(m, n) zero) of the m x n column-major A,
+// by a TSQR reduction of single-block Householder QRs (blocks of max(2n, 256) rows, then pairs of
+// stacked R factors): backward stable for any rank, every level one batched launch.
+void qr_r(const double* A, int64_t lda, int64_t m, int64_t n, double* R, LinalgWS& ws,
+          cudaStream_t s);
+
 // Thin SVD A = U diag(S) Vh of the m x n column-major matrix A (lda): U (m x k, ld m),
 // S (k), Vh (k x n, ld k), k = min(m, n), singular values in descending order.
 // (reference: at::linalg_svd(A, full_matrices=false))

@@ -69,7 +69,7 @@ std::vector<DTensor> tt_matvec(const TTView& A, const TTView& x, cudaStream_t s,
 double tt_norm(const TTView& x, LinalgWS& ws, const RedWS& red, cudaStream_t s) {
   const int d = x.d;
   TTGB_REQUIRE(d >= 1, "empty TT");
-  DBuf T, Q, Rf, CT, out;
+  DBuf T, Rf, CT, out;
   out.reset(1, s);
   // CT = Cur^T (rc x R_{k+1}, column-major, ld rc), Cur = I_1 at the right end
   int64_t rc = 1;
@@ -90,14 +90,14 @@ double tt_norm(const TTView& x, LinalgWS& ws, const RedWS& red, cudaStream_t s) 
       nrm2(red, W, m * r, out.p, s);
       break;
     }
-    const int64_t kk = std::min(m, r);
-    Q.ensure((size_t)m * kk, s);
-    Rf.ensure((size_t)kk * r, s);
-    qr(W, m, m, r, Q.p, Rf.p, ws, red, s);
-    // Cur_new = Rf^T (r x kk): CT_new = Rf (kk x r, ld kk)
-    CT.ensure((size_t)kk * r, s);
-    copy(Rf.p, CT.p, kk * r, s);
-    rc = kk;
+    // R factor of the unfolding by TSQR (robust when it is rank deficient, as the unfoldings of
+    // a residual A x - b are): an r x r upper block, rows past min(m, r) zero
+    Rf.ensure((size_t)r * r, s);
+    qr_r(W, m, m, r, Rf.p, ws, s);
+    // Cur_new = Rf^T (r x r): CT_new = Rf (r x r, ld r)
+    CT.ensure((size_t)r * r, s);
+    copy(Rf.p, CT.p, r * r, s);
+    rc = r;
   }
   double h = 0.0;
   TTGB_CUDA(cudaMemcpyAsync(&h, out.p, sizeof(double), cudaMemcpyDeviceToHost, s));

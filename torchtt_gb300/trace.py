@@ -29,12 +29,14 @@ def _percentile(xs, q):
 
 
 def replay(count, rate, slots=8, precision="mixed", engine="auto", seed=5, mem_budget_bytes=0,
-           check=True, device=None):
+           check=True, device=None, max_d=24, ranks=(1, 32), modes=(16, 32, 64)):
+    """Replays ``count`` requests arriving at ``rate`` per second; ``max_d``, ``ranks`` and
+    ``modes`` bound the request sizes (full size: 24, (1, 32), (16, 32, 64))."""
     dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
     trace = W.serving_trace(count, rate, seed)
     reqs = []
     for t_arr, i in trace:   # inputs prepared on the device before the clock starts
-        w = W.serving_request(i, seed)
+        w = W.serving_request(i, seed, max_d=max_d, ranks=ranks, modes=modes)
         A = TT([c.to(dev) for c in w["A"]])
         b = TT([c.to(dev) for c in w["b"]])
         reqs.append((t_arr, i, w, A, b))
@@ -75,10 +77,13 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--engine", default="auto", choices=["auto", "tc", "fp32"])
     ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--max-d", type=int, default=24)
+    ap.add_argument("--max-rank", type=int, default=32)
     ap.add_argument("--no-check", action="store_true")
     args = ap.parse_args()
     print(json.dumps(replay(args.requests, args.rate, args.slots, args.precision, args.engine,
-                            args.seed, check=not args.no_check)))
+                            args.seed, check=not args.no_check, max_d=args.max_d,
+                            ranks=(1, args.max_rank))))
 
 
 if __name__ == "__main__":

@@ -235,27 +235,29 @@ def small_random_system(seed=0, N=(4, 5, 6), RA=(1, 2, 3, 1), RX=(1, 2, 3, 1)):
                 x=_to_torch(x), x0=None, params=dict(eps=1e-10))
 
 
-def rounding_stress_d16_n32(index, seed=4):
-    """One solve of the 128-solve rounding batch: d=16, n=32, A = Laplacian + C C^T + I (C a random
-    rank-2 TT-matrix with N(0, 0.01^2) cores, so the perturbation has rank 4 and A is SPD); b = the
-    sum of 4 random rank-16 TTs (input rank 64, N(0,1) cores), to be rounded to ``round_b`` before
-    the solve; eps 1e-8."""
-    d, n = 16, 32
+def rounding_stress(index, seed=4, d=16, n=32, term_rank=16, terms=4, kickrank=8, nswp=20):
+    """One solve of the rounding batch (full size: 128 solves, d=16, n=32, 4 rank-16 terms):
+    A = Laplacian + C C^T + I (C a random rank-2 TT-matrix with N(0, 0.01^2) cores, so the
+    perturbation has rank 4 and A is SPD); b = the sum of ``terms`` random TTs of rank
+    ``term_rank`` (N(0,1) cores), to be rounded to ``round_b`` before the solve; eps 1e-8.
+    AMEn grows the solution ranks by at most ``kickrank`` per sweep, so a right-hand side of rank
+    64 needs nswp * kickrank well above the rank of the solution to converge."""
     A = laplace_lowrank_spd_ttm(d, n, seed)
-    parts = [random_tt([n] * d, [1] + [16] * (d - 1) + [1], seed * 100003 + 4 * index + i,
-                       normalise=False) for i in range(4)]
-    return dict(name="rounding_stress_d16_n32", A=A, b=tt_sum(parts), x0=None, round_b=1e-8,
-                params=dict(eps=1e-8, nswp=20, kickrank=8))
+    parts = [random_tt([n] * d, [1] + [term_rank] * (d - 1) + [1], seed * 100003 + terms * index + i,
+                       normalise=False) for i in range(terms)]
+    return dict(name="rounding_stress_d%d_n%d" % (d, n), A=A, b=tt_sum(parts), x0=None,
+                round_b=1e-8, params=dict(eps=1e-8, nswp=nswp, kickrank=kickrank))
 
 
-def serving_request(index, seed=5):
-    """One request of the serving trace: d ~ U{8..24}, n in {16, 32, 64}, rhs rank ~ U{1..32}
+def serving_request(index, seed=5, max_d=24, ranks=(1, 32), modes=(16, 32, 64)):
+    """One request of the serving trace: d ~ U{8..max_d}, n in ``modes``, rhs rank ~ U{ranks}
     (N(0,1) cores, ||b|| = 1), operator = anisotropic Laplacian sum_k c_k L_k with c_k ~ U[0.1, 10],
-    eps in {1e-6, 1e-8, 1e-10}; the reference's other defaults."""
+    eps in {1e-6, 1e-8, 1e-10}; the reference's other defaults. Full size: max_d 24, ranks 1..32,
+    n in {16, 32, 64}."""
     g = _rng(seed * 1000003 + index)
-    d = int(g.integers(8, 25))
-    n = int(g.choice([16, 32, 64]))
-    r = int(g.integers(1, 33))
+    d = int(g.integers(8, max_d + 1))
+    n = int(g.choice(list(modes)))
+    r = int(g.integers(ranks[0], ranks[1] + 1))
     coeffs = g.uniform(0.1, 10.0, size=d)
     eps = float(g.choice([1e-6, 1e-8, 1e-10]))
     A = laplace_ttm(d, n, coeffs=coeffs)
