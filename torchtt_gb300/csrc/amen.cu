@@ -640,20 +640,40 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
       lrhs(Phis_b_[k].data(), rk, k, Phiz_b_[k + 1].data(), rzk1, nrmsc_, left_b.p);
       axpby(-1.0, left_res.p, 1.0, left_b.p, a * rzk1, s_);   // uk = left_b - left_res
       const int64_t nc = r + rzk1;
-      DBuf UK((size_t)(a * nc), s_);
-      copy(U.p, UK.p, a * r, s_);
-      transpose(left_b.p, rzk1, UK.p + a * r, a, rzk1, a, s_);
       k2 = a < nc ? a : nc;
-      DBuf Qn((size_t)(a * k2), s_), Rm((size_t)(k2 * nc), s_);
-      qr(UK.p, a, a, nc, Qn.p, Rm.p, lws_, red_, s_);
-      // V'[i, j] = sum_{q<r} SVh[q + i kf] Rm[j + q k2]
+      DBuf Qn((size_t)(a * k2), s_);
       vprime.reset((size_t)(bdim * k2), s_);
-      ContractDesc cd;
-      cd.M = (int)bdim; cd.N = (int)k2; cd.K = (int)r;
-      cd.A = SVh.p; cd.am = Ax::one(kf); cd.ak = Ax::one(1);
-      cd.B = Rm.p; cd.bk = Ax::one(k2); cd.bn = Ax::one(1);
-      cd.C = vprime.p; cd.cm = Ax::one(1); cd.cn = Ax::one(bdim);
-      contract(cd, s_);
+      if (a >= nc) {
+        // The first r columns U are orthonormal (left singular vectors), so QR([U, Z]) is
+        // [U, Q_z] [[I, C], [0, R_z]] with C = U^T Z and Q_z R_z = (I - U U^T) Z: the block
+        // Gram-Schmidt of the rzk1 residual columns against U (applied twice, CGS2) and a small
+        // QR replace a CholeskyQR3 of all r + rzk1 columns; the span, hence the TT, is the same
+        // as the reference's QR of the stacked block (amen_solve.h:452-458).
+        DBuf Z((size_t)(a * rzk1), s_), Cm((size_t)(r * rzk1), s_);
+        transpose(left_b.p, rzk1, Z.p, a, rzk1, a, s_);                  // Z: a x rzk1, ld a
+        for (int pass = 0; pass < 2; ++pass) {
+          gemm_cm(U.p, a, Z.p, a, Cm.p, r, r, rzk1, a, 1.0, 0.0, s_, true, false);    // U^T Z
+          gemm_cm(U.p, a, Cm.p, r, Z.p, a, a, rzk1, r, -1.0, 1.0, s_);                 // Z -= U C
+        }
+        DBuf Rz((size_t)(rzk1 * rzk1), s_);
+        qr(Z.p, a, a, rzk1, Qn.p + a * r, Rz.p, lws_, red_, s_);
+        copy(U.p, Qn.p, a * r, s_);
+        // V' = SVh^T Rm[:, :r]^T = [SVh^T, 0]: V'[i, j] = SVh[j + i kf] for j < r
+        fill(vprime.p, 0.0, bdim * k2, s_);
+        transpose(SVh.p, kf, vprime.p, bdim, r, bdim, s_);
+      } else {
+        DBuf UK((size_t)(a * nc), s_), Rm((size_t)(k2 * nc), s_);
+        copy(U.p, UK.p, a * r, s_);
+        transpose(left_b.p, rzk1, UK.p + a * r, a, rzk1, a, s_);
+        qr(UK.p, a, a, nc, Qn.p, Rm.p, lws_, red_, s_);
+        // V'[i, j] = sum_{q<r} SVh[q + i kf] Rm[j + q k2]
+        ContractDesc cd;
+        cd.M = (int)bdim; cd.N = (int)k2; cd.K = (int)r;
+        cd.A = SVh.p; cd.am = Ax::one(kf); cd.ak = Ax::one(1);
+        cd.B = Rm.p; cd.bk = Ax::one(k2); cd.bn = Ax::one(1);
+        cd.C = vprime.p; cd.cm = Ax::one(1); cd.cn = Ax::one(bdim);
+        contract(cd, s_);
+      }
       newx.reset((size_t)(a * k2), s_);
       transpose(Qn.p, a, newx.p, k2, a, k2, s_);
     } else {

@@ -84,17 +84,18 @@ __global__ void __launch_bounds__(512) chol_kernel(double* G, int n, int64_t shi
     for (int i = tid; i < n; i += nt) G[(int64_t)i * n + i] += sft;
   }
   __syncthreads();
+  __shared__ double piv_inv;   // pivot reciprocal, computed once per step (see chol_inv_smem)
   for (int j = 0; j < n; ++j) {
-    const double d = G[(int64_t)j * n + j];
-    if (!(d > 0.0) || !isfinite(d)) {
-      if (tid == 0) { bad = 1; *status = 1; }
+    if (tid == 0) {
+      const double d = G[(int64_t)j * n + j];
+      if (!(d > 0.0) || !isfinite(d)) { bad = 1; *status = 1; }
+      else { const double rd = sqrt(d); G[(int64_t)j * n + j] = rd; piv_inv = 1.0 / rd; }
     }
     __syncthreads();
     if (bad) break;
-    const double rd = sqrt(d);
-    for (int k = j + 1 + tid; k < n; k += nt) G[(int64_t)j * n + k] /= rd;
+    const double inv = piv_inv;
+    for (int k = j + 1 + tid; k < n; k += nt) G[(int64_t)j * n + k] *= inv;
     __syncthreads();
-    if (tid == 0) G[(int64_t)j * n + j] = rd;
     const int w = n - j - 1;
     for (int64_t t = tid; t < (int64_t)w * w; t += nt) {
       const int i = j + 1 + (int)(t / w), k = j + 1 + (int)(t % w);
@@ -148,19 +149,21 @@ __global__ void __launch_bounds__(512) chol_inv_smem_kernel(const double* __rest
     for (int i = tid; i < n; i += nt) G[i * ld + i] += sft;
   }
   __syncthreads();
-  // right-looking Cholesky, upper triangle only
+  // right-looking Cholesky, upper triangle only. The pivot's square root and reciprocal are
+  // computed once per step by one thread: FP64 sqrt and division expand to several DFMA, and 16
+  // warps computing them redundantly would occupy the SM's FP64 pipe for thousands of cycles.
+  __shared__ double piv_inv;
   for (int j = 0; j < n; ++j) {
-    const double d = G[j * ld + j];
-    if (!(d > 0.0) || !isfinite(d)) {
-      if (tid == 0) { bad = 1; *status = 1; }
+    if (tid == 0) {
+      const double d = G[j * ld + j];
+      if (!(d > 0.0) || !isfinite(d)) { bad = 1; *status = 1; }
+      else { const double rd = sqrt(d); G[j * ld + j] = rd; piv_inv = 1.0 / rd; }
     }
     __syncthreads();
     if (bad) break;
-    const double rd = sqrt(d);
-    const double inv = 1.0 / rd;
+    const double inv = piv_inv;
     for (int k = j + 1 + tid; k < n; k += nt) G[j * ld + k] *= inv;
     __syncthreads();
-    if (tid == 0) G[j * ld + j] = rd;
     {   // trailing update of the upper triangle: one warp per row, lanes over columns
       const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
       for (int i = j + 1 + warp; i < n; i += nw) {
@@ -187,7 +190,9 @@ __global__ void __launch_bounds__(512) chol_inv_smem_kernel(const double* __rest
   {
     const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     for (int j = n - 1; j >= 0; --j) {
-      const double inv = 1.0 / G[j * ld + j];
+      if (tid == 0) piv_inv = 1.0 / G[j * ld + j];
+      __syncthreads();
+      const double inv = piv_inv;
       for (int k = j + tid; k < n; k += nt) X[j * ld + k] *= inv;
       __syncthreads();
       for (int i = warp; i < j; i += nw) {
@@ -230,6 +235,7 @@ __global__ void trinv_kernel(const double* __restrict__ R, double* Ri, int n) {
 __global__ void __launch_bounds__(512) householder_kernel(double* W, int m, int n, double* Q,
                                                           double* R, double* tau) {
   __shared__ double sh[32];
+  __shared__ double refl[3];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   const int k = min(m, n);
@@ -238,14 +244,18 @@ __global__ void __launch_bounds__(512) householder_kernel(double* W, int m, int 
     double xs = 0.0;
     for (int i = j + 1 + tid; i < m; i += nt) xs = fma(col[i], col[i], xs);
     xs = block_sum_d(xs, sh);
-    const double alpha = col[j];
-    const double nrm = sqrt(alpha * alpha + xs);
-    double tj = 0.0, beta = alpha, scale = 0.0;
-    if (xs > 0.0) {
-      beta = -copysign(nrm, alpha);
-      tj = (beta - alpha) / beta;
-      scale = 1.0 / (alpha - beta);
+    if (tid == 0) {   // reflector scalars once per column (FP64 sqrt/division are DFMA sequences)
+      const double alpha = col[j];
+      double tj = 0.0, beta = alpha, scale = 0.0;
+      if (xs > 0.0) {
+        beta = -copysign(sqrt(alpha * alpha + xs), alpha);
+        tj = (beta - alpha) / beta;
+        scale = 1.0 / (alpha - beta);
+      }
+      refl[0] = tj; refl[1] = beta; refl[2] = scale;
     }
+    __syncthreads();
+    const double tj = refl[0], beta = refl[1], scale = refl[2];
     for (int i = j + 1 + tid; i < m; i += nt) col[i] *= scale;
     __syncthreads();
     if (tid == 0) { col[j] = beta; tau[j] = tj; }
@@ -302,6 +312,7 @@ __global__ void __launch_bounds__(512) householder_kernel(double* W, int m, int 
 __global__ void __launch_bounds__(512) householder_r_kernel(double* Wall, int64_t stride, int rows,
                                                             int n, double* Rout) {
   __shared__ double sh[32];
+  __shared__ double refl[3];
   double* W = Wall + (int64_t)blockIdx.x * stride;
   double* R = Rout + (int64_t)blockIdx.x * n * n;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -312,14 +323,18 @@ __global__ void __launch_bounds__(512) householder_r_kernel(double* Wall, int64_
     double xs = 0.0;
     for (int i = j + 1 + tid; i < rows; i += nt) xs = fma(col[i], col[i], xs);
     xs = block_sum_d(xs, sh);
-    const double alpha = col[j];
-    const double nrm = sqrt(alpha * alpha + xs);
-    double tj = 0.0, beta = alpha, scale = 0.0;
-    if (xs > 0.0) {
-      beta = -copysign(nrm, alpha);
-      tj = (beta - alpha) / beta;
-      scale = 1.0 / (alpha - beta);
+    if (tid == 0) {   // reflector scalars once per column (FP64 sqrt/division are DFMA sequences)
+      const double alpha = col[j];
+      double tj = 0.0, beta = alpha, scale = 0.0;
+      if (xs > 0.0) {
+        beta = -copysign(sqrt(alpha * alpha + xs), alpha);
+        tj = (beta - alpha) / beta;
+        scale = 1.0 / (alpha - beta);
+      }
+      refl[0] = tj; refl[1] = beta; refl[2] = scale;
     }
+    __syncthreads();
+    const double tj = refl[0], beta = refl[1], scale = refl[2];
     for (int i = j + 1 + tid; i < rows; i += nt) col[i] *= scale;
     __syncthreads();
     if (tid == 0) col[j] = beta;
@@ -377,6 +392,44 @@ __global__ void tsqr_stack_kernel(const double* __restrict__ R, int n, int nin, 
 // Appl. 13, 1992). On exit U (n x n) holds W_j / sigma_j, V the accumulated rotations, both with
 // columns sorted by descending sigma, S the sorted singular values.
 // ---------------------------------------------------------------------------------------------
+// Rotation (c, s) of one-sided Jacobi for a column pair with squared norms a, b and inner product
+// g (Demmel-Veselic formulas): false when the pair is orthogonal to `tol`. The tangent t of the
+// angle comes from FP32 arithmetic (relative error ~1e-7: the pair is left orthogonal to ~1e-7 and
+// a later sweep finishes it), and c = 1/sqrt(1 + t^2) is refined from the FP32 rsqrt to full FP64
+// accuracy by two Newton steps, so (c, s) is orthogonal to rounding. On GB300 an FP64 sqrt or
+// division is a sequence of DFMA on a pipe that issues one warp instruction per 16 cycles; the
+// exact formula costs ~4 sqrt + 3 divisions per rotation, this one ~8 DFMA.
+__device__ __forceinline__ bool jacobi_rotation(double a, double b, double g, double tol, double& c,
+                                                double& s) {
+  if (a == 0.0 || b == 0.0) return false;
+  if (!(g * g > tol * tol * a * b)) return false;
+  const double bma = b - a, g2 = 2.0 * g;
+  const float fb = (float)bma, fg = (float)g2;
+  float tf;
+  if (fabsf(fb) >= fabsf(fg)) {   // r = 2g / (b - a), |r| <= 1: t = r / (1 + sqrt(1 + r^2))
+    const float r = __fdividef(fg, fb);
+    tf = __fdividef(r, 1.0f + sqrtf(fmaf(r, r, 1.0f)));
+  } else {                        // zeta = (b - a) / 2g, |zeta| < 1
+    const float z = __fdividef(fb, fg);
+    tf = __fdividef(copysignf(1.0f, z), fabsf(z) + sqrtf(fmaf(z, z, 1.0f)));
+  }
+  double t;
+  if (tf != 0.0f && isfinite(tf)) {
+    t = (double)tf;
+  } else {   // operands outside the FP32 range: the exact FP64 formula
+    const double zeta = bma / g2;
+    t = (fabs(zeta) > 1e150) ? 0.5 / zeta
+                             : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+  }
+  const double x = fma(t, t, 1.0);
+  double y = (double)rsqrtf((float)x);
+  y = y * fma(-0.5 * x, y * y, 1.5);
+  y = y * fma(-0.5 * x, y * y, 1.5);
+  c = y;
+  s = y * t;
+  return true;
+}
+
 __device__ __forceinline__ int rr_index(int p, int r, int nn) {
   return p == 0 ? 0 : ((p - 1 + r) % (nn - 1)) + 1;
 }
@@ -415,13 +468,8 @@ __global__ void __launch_bounds__(512) jacobi_svd_kernel(double* Wg, double* Vg,
           a = fma(x, x, a); b = fma(y, y, b); g = fma(x, y, g);
         }
         a = warp_sum_d(a); b = warp_sum_d(b); g = warp_sum_d(g);
-        if (a == 0.0 || b == 0.0) continue;
-        if (!(fabs(g) > tol * sqrt(a) * sqrt(b))) continue;
-        const double zeta = (b - a) / (2.0 * g);
-        double t;
-        if (fabs(zeta) > 1e150) t = 0.5 / zeta;
-        else t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+        double c, s;
+        if (!jacobi_rotation(a, b, g, tol, c, s)) continue;
         for (int i = lane; i < n; i += 32) {
           const double x = wp[i], y = wq[i];
           wp[i] = c * x - s * y;
@@ -541,12 +589,8 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
           a = fma(x, x, a); b = fma(y, y, b); g = fma(x, y, g);
         }
         a = warp_sum_d(a); b = warp_sum_d(b); g = warp_sum_d(g);
-        if (a == 0.0 || b == 0.0) continue;
-        if (!(fabs(g) > tol * sqrt(a) * sqrt(b))) continue;
-        const double zeta = (b - a) / (2.0 * g);
-        const double t = (fabs(zeta) > 1e150) ? 0.5 / zeta
-                                               : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+        double c, s;
+        if (!jacobi_rotation(a, b, g, tol, c, s)) continue;
         for (int i = lane; i < n; i += 32) {
           const double x = wp[i], y = wq[i];
           wp[i] = c * x - s * y;
@@ -601,12 +645,8 @@ __device__ __forceinline__ int jacobi_rotate_pair(double* wp, double* wq, double
     a = fma(x, x, a); b = fma(y, y, b); g = fma(x, y, g);
   }
   a = warp_sum_d(a); b = warp_sum_d(b); g = warp_sum_d(g);
-  if (a == 0.0 || b == 0.0) return 0;
-  if (!(fabs(g) > tol * sqrt(a) * sqrt(b))) return 0;
-  const double zeta = (b - a) / (2.0 * g);
-  const double t = (fabs(zeta) > 1e150) ? 0.5 / zeta
-                                         : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-  const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+  double c, s;
+  if (!jacobi_rotation(a, b, g, tol, c, s)) return 0;
   for (int i = lane; i < n; i += 32) {
     const double x = wp[i], y = wq[i];
     wp[i] = c * x - s * y;
@@ -777,6 +817,7 @@ __global__ void __launch_bounds__(1024) svd_sort_kernel(const double* __restrict
 // ---------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) lu_solve_kernel(double* LU, double* x, int n, int* status) {
   __shared__ double shv[32];
+  __shared__ double piv_inv;
   __shared__ int shi[32];
   __shared__ int piv;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -815,10 +856,12 @@ __global__ void __launch_bounds__(1024) lu_solve_kernel(double* LU, double* x, i
       if (tid == 0) { const double t = x[j]; x[j] = x[p]; x[p] = t; }
     }
     __syncthreads();
-    const double dj = LU[(int64_t)j * n + j];
+    if (tid == 0) piv_inv = 1.0 / LU[(int64_t)j * n + j];   // one FP64 division per step
+    __syncthreads();
+    const double inv = piv_inv;
     const int w = n - j - 1;
     // multipliers
-    for (int i = j + 1 + tid; i < n; i += nt) LU[(int64_t)i * n + j] /= dj;
+    for (int i = j + 1 + tid; i < n; i += nt) LU[(int64_t)i * n + j] *= inv;
     __syncthreads();
     for (int i = j + 1 + tid; i < n; i += nt) x[i] = fma(-LU[(int64_t)i * n + j], x[j], x[i]);
     for (int64_t t = tid; t < (int64_t)w * w; t += nt) {

@@ -59,36 +59,56 @@ __device__ __forceinline__ int64_t tc_off(const TcAx& a, int i) {
   return (int64_t)i1 * a.s1 + (int64_t)i0 * a.s0;
 }
 
-// stage rows [row0, row0 + rows) x K chunk [k0, k0 + 32) of a K-major matrix into the swizzled tile
-__device__ __forceinline__ void stage_tile(const float* __restrict__ src, int64_t ld, int nrows_valid,
-                                           int row0, int rows, int K, int k0, float* dst) {
-  for (int c = threadIdx.x; c < rows * 8; c += kThreads) {
-    const int r = c >> 3, ch = c & 7;
-    const int gr = row0 + r, k = k0 + ch * 4;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (gr < nrows_valid) {
-      const float* p = src + (int64_t)gr * ld + k;
-      if (k + 3 < K) {
-        v.x = p[0]; v.y = p[1]; v.z = p[2]; v.w = p[3];
-      } else {
-        if (k < K) v.x = p[0];
-        if (k + 1 < K) v.y = p[1];
-        if (k + 2 < K) v.z = p[2];
+// Asynchronous copies global -> shared (cp.async): the issuing thread does not wait, so every
+// element of a K chunk is in flight at once; a source size below the copy size zero-fills.
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float* src, int bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(uint32_t dst, const float* src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes)
+               : "memory");
+}
+
+// Stage rows [row0, row0 + rows) x K chunk [k0, k0 + 32) of a K-major matrix into the 128-byte
+// swizzled tile (16-byte granule c of row r at granule c ^ (r & 7)). VEC: 16-byte copies (rows
+// and the matrix 16-byte aligned); otherwise 4-byte copies.
+template <bool VEC>
+__device__ __forceinline__ void stage_async(const float* __restrict__ src, int64_t ld,
+                                            int nrows_valid, int row0, int rows, int K, int k0,
+                                            float* dst) {
+  if constexpr (VEC) {
+    for (int c = threadIdx.x; c < rows * 8; c += kThreads) {
+      const int r = c >> 3, ch = c & 7;
+      const int gr = row0 + r, k = k0 + ch * 4;
+      int bytes = 0;
+      const float* p = src;
+      if (gr < nrows_valid && k < K) {
+        bytes = (K - k >= 4 ? 4 : K - k) * 4;
+        p = src + (int64_t)gr * ld + k;
       }
+      cp_async16(smem_u32(dst + r * kBK + ((ch ^ (r & 7)) << 2)), p, bytes);
     }
-    *reinterpret_cast<float4*>(dst + r * kBK + ((ch ^ (r & 7)) << 2)) = v;
+  } else {
+    for (int c = threadIdx.x; c < rows * kBK; c += kThreads) {
+      const int r = c >> 5, kk = c & 31;
+      const int gr = row0 + r, k = k0 + kk;
+      const bool ok = gr < nrows_valid && k < K;
+      cp_async4(smem_u32(dst + r * kBK + (((kk >> 2) ^ (r & 7)) << 2) + (kk & 3)),
+                ok ? src + (int64_t)gr * ld + k : src, ok ? 4 : 0);
+    }
   }
 }
 
-template <int BN>
+// K loop with two shared-memory stages: the copies of chunk k+1 are issued before the MMAs of
+// chunk k, and a stage is refilled only after the MMAs that read it have committed (mbarrier).
+template <int BN, bool VEC>
 __global__ void __launch_bounds__(kThreads) tc_gemm_kernel(TcGemm g, int* err) {
   extern __shared__ uint8_t smraw[];
   uint8_t* smbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
-  float* sAh = reinterpret_cast<float*>(smbase);
-  float* sAl = sAh + kBM * kBK;
-  float* sBh = sAl + kBM * kBK;
-  float* sBl = sBh + BN * kBK;
-  __shared__ __align__(8) uint64_t mbar;
+  constexpr int kStage = 2 * kBM * kBK + 2 * BN * kBK;   // floats per stage: A hi/lo, B hi/lo
+  float* const stage0 = reinterpret_cast<float*>(smbase);
+  __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
   constexpr uint32_t kCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
@@ -102,7 +122,8 @@ __global__ void __launch_bounds__(kThreads) tc_gemm_kernel(TcGemm g, int* err) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])));
     asm volatile("fence.mbarrier_init.release.cluster;");
     abort_sh = 0;
   }
@@ -110,7 +131,7 @@ __global__ void __launch_bounds__(kThreads) tc_gemm_kernel(TcGemm g, int* err) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_sh;
-  const uint32_t bar = smem_u32(&mbar);
+  const uint32_t bar[2] = {smem_u32(&mbar[0]), smem_u32(&mbar[1])};
 
   const float* Ah = g.A_hi + (int64_t)bz * g.a_bs;
   const float* Al = g.A_lo + (int64_t)bz * g.a_bs;
@@ -118,19 +139,45 @@ __global__ void __launch_bounds__(kThreads) tc_gemm_kernel(TcGemm g, int* err) {
   const float* Bl = g.B_lo + (int64_t)bz * g.b_bs;
   const uint32_t idesc = idesc_tf32(BN);
   const int nk = (g.K + kBK - 1) / kBK;
-  uint32_t parity = 0;
-  bool ok = true;
-  for (int kc = 0; kc < nk; ++kc) {
+
+  auto issue = [&](int kc, int st) {
     const int k0 = kc * kBK;
-    stage_tile(Ah, g.lda, g.M, m0, kBM, g.K, k0, sAh);
-    stage_tile(Al, g.lda, g.M, m0, kBM, g.K, k0, sAl);
-    stage_tile(Bh, g.ldb, g.N, n0, BN, g.K, k0, sBh);
-    stage_tile(Bl, g.ldb, g.N, n0, BN, g.K, k0, sBl);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic writes -> async proxy
+    float* sAh = stage0 + st * kStage;
+    float* sAl = sAh + kBM * kBK;
+    float* sBh = sAl + kBM * kBK;
+    float* sBl = sBh + BN * kBK;
+    stage_async<VEC>(Ah, g.lda, g.M, m0, kBM, g.K, k0, sAh);
+    stage_async<VEC>(Al, g.lda, g.M, m0, kBM, g.K, k0, sAl);
+    stage_async<VEC>(Bh, g.ldb, g.N, n0, BN, g.K, k0, sBh);
+    stage_async<VEC>(Bl, g.ldb, g.N, n0, BN, g.K, k0, sBl);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  uint32_t phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};   // a commit on this barrier has not been waited for
+  bool ok = true;
+  issue(0, 0);
+  for (int kc = 0; kc < nk; ++kc) {
+    const int st = kc & 1;
+    if (kc + 1 < nk) {
+      if (pending[st ^ 1]) {   // the MMAs of chunk kc-1 read stage st^1: wait before refilling it
+        if (!mbar_wait(bar[st ^ 1], phase[st ^ 1])) abort_sh = 1;
+        phase[st ^ 1] ^= 1u;
+        pending[st ^ 1] = false;
+      }
+      issue(kc + 1, st ^ 1);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // copies -> async proxy
     __syncthreads();
+    if (abort_sh) { ok = false; break; }
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t ah = smem_u32(sAh), al = smem_u32(sAl), bh = smem_u32(sBh), bl = smem_u32(sBl);
+      const float* sAh = stage0 + st * kStage;
+      const uint32_t ah = smem_u32(sAh), al = smem_u32(sAh + kBM * kBK);
+      const uint32_t bh = smem_u32(sAh + 2 * kBM * kBK), bl = smem_u32(sAh + 2 * kBM * kBK + BN * kBK);
 #pragma unroll
       for (int kk = 0; kk < kBK / 8; ++kk) {   // K = 8 TF32 (32 bytes) per instruction
         const uint32_t o = kk * 32;
@@ -138,15 +185,19 @@ __global__ void __launch_bounds__(kThreads) tc_gemm_kernel(TcGemm g, int* err) {
         mma_tf32(tmem, desc_sw128(ah + o), desc_sw128(bl + o), idesc, 1u);
         mma_tf32(tmem, desc_sw128(al + o), desc_sw128(bh + o), idesc, 1u);
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar[st])
                    : "memory");
     }
-    // the MMAs read the staged tiles: wait for them before the next chunk is written
-    if (!mbar_wait(bar, parity)) abort_sh = 1;
-    parity ^= 1u;
-    __syncthreads();
-    if (abort_sh) { ok = false; break; }
+    pending[st] = true;
   }
+  if (ok) {   // the last commit covers every MMA issued before it
+    const int st = (nk - 1) & 1;
+    if (!mbar_wait(bar[st], phase[st])) abort_sh = 1;
+    pending[0] = pending[1] = false;
+    __syncthreads();
+    if (abort_sh) ok = false;
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (ok) {
     const int row = m0 + warp * 32 + lane;
@@ -186,7 +237,8 @@ __global__ void __launch_bounds__(kThreads) tc_gemm_kernel(TcGemm g, int* err) {
   } else if (tid == 0) {
     atomicExch(err, 1);
     // give MMAs still in flight a bounded chance to finish before their accumulator is released
-    mbar_wait(bar, parity ^ 1u);
+    for (int b = 0; b < 2; ++b)
+      if (pending[b]) mbar_wait(bar[b], phase[b]);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -210,13 +262,23 @@ __global__ void split_tf32_kernel(const double* __restrict__ x, Gather4 g, float
   }
 }
 
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 template <int BN>
 void launch(const TcGemm& g, int* err, cudaStream_t s) {
-  const size_t smem = (size_t)(2 * kBM * kBK + 2 * BN * kBK) * sizeof(float) + 1024;
-  smem_optin((const void*)tc_gemm_kernel<BN>, (int)smem);
+  const size_t smem = (size_t)2 * (2 * kBM * kBK + 2 * BN * kBK) * sizeof(float) + 1024;
   dim3 grid(cdiv(g.N, BN), cdiv(g.M, kBM), (unsigned)g.batch);
   TTGB_REQUIRE(grid.y < 65536 && grid.z < 65536, "tc_gemm grid too large");
-  tc_gemm_kernel<BN><<<grid, kThreads, smem, s>>>(g, err);
+  // 16-byte copies when every row of both operands starts on a 16-byte boundary
+  const bool vec = aligned16(g.A_hi) && aligned16(g.A_lo) && aligned16(g.B_hi) && aligned16(g.B_lo) &&
+                   g.lda % 4 == 0 && g.ldb % 4 == 0 && g.a_bs % 4 == 0 && g.b_bs % 4 == 0;
+  if (vec) {
+    smem_optin((const void*)tc_gemm_kernel<BN, true>, (int)smem);
+    tc_gemm_kernel<BN, true><<<grid, kThreads, smem, s>>>(g, err);
+  } else {
+    smem_optin((const void*)tc_gemm_kernel<BN, false>, (int)smem);
+    tc_gemm_kernel<BN, false><<<grid, kThreads, smem, s>>>(g, err);
+  }
   TTGB_CHECK_LAUNCH();
 }
 
