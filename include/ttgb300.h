@@ -68,6 +68,11 @@ typedef struct ttgb_amen_params {
                                    TTGB_ENGINE_FP32 or TTGB_ENGINE_TC */
   int32_t a_structure;          /* 1 (default): A cores with density < 1/4 (Kronecker-sum
                                    operators) are applied from their nonzeros; 0: always dense */
+  int32_t fp64_engine;          /* FP64 products of local matvecs, interfaces and local rhs:
+                                   0 auto (double-float arithmetic on the FP32 pipe on the MIXED
+                                   path when A and b fit the FP32 exponent range, ~1e-13
+                                   relative; native FP64 otherwise), 1 native FP64, 2 double-float.
+                                   QR and SVD always run in native FP64. */
 } ttgb_amen_params;
 
 /* Precision modes. FP64: the reference's arithmetic. MIXED: the local GMRES applies the projected

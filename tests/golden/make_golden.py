@@ -9,6 +9,7 @@ Python package is imported from the tree. Writes ``tests/golden/*.npz``:
   seeded random shapes, plus a GMRES known answer (``torchtt/_iterative_solvers.py:72-158`` on a
   1-D Laplacian, the pattern of ``cpp/test_gmres.cpp:187-253``);
 * ``round.npz`` - inputs and outputs of the reference's TT rounding (``TT.round``);
+* ``divide.npz`` - inputs and outputs of the reference's elementwise division (``amen_divide``);
 * ``solve_<name>.npz`` - the inputs of a whole solve (A, b, x0 cores, the initial enrichment cores z0
   that the reference drew with ``torch::randn`` after ``torch.manual_seed``), the parameters, and the
   solution cores returned by ``torchttcpp.amen_solve`` (``cpp/amen_solve.h:122``) and, for the small
@@ -115,6 +116,28 @@ def rounding(torchtt):
     print("round.npz written")
 
 
+def division(torchtt):
+    """Elementwise division by the reference's amen_divide (torchtt/_division.py:76): a = 1 + a
+    small random TT (no zeros), b random; the reference's own random start is not recorded (its z
+    cores come from the global torch RNG), so parity is on the solution."""
+    from torchtt._division import amen_divide
+    out = {}
+    cases = [("d3", [6, 7, 8], [1, 2, 2, 1], [1, 3, 3, 1]), ("d6", [8] * 6, [1] + [2] * 5 + [1], [1] + [3] * 5 + [1])]
+    for name, N, Ra, Rb in cases:
+        d = len(N)
+        one = torchtt.TT([torch.ones((1, n, 1), dtype=torch.float64) for n in N])
+        a = one + torchtt.TT(W.random_tt(N, Ra, 71 + d)) * 0.5
+        b = torchtt.TT(W.random_tt(N, Rb, 81 + d))
+        torch.manual_seed(3)
+        x = amen_divide(a, b, nswp=22, eps=1e-10, verbose=False)
+        _pack_cores(name + "_a", a.cores, out)
+        _pack_cores(name + "_b", b.cores, out)
+        _pack_cores(name + "_x", x, out)
+    out["names"] = np.array([c[0] for c in cases])
+    np.savez_compressed(os.path.join(HERE, "divide.npz"), **out)
+    print("divide.npz written")
+
+
 def solve_case(torchtt, cpp, wl, seed, prec=None, with_python=False, extra=None):
     A, b, x0 = wl["A"], wl["b"], wl.get("x0")
     p = dict(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
@@ -167,6 +190,7 @@ def main():
     torchtt, cpp = build_ref.load_reference_package()
     kernels(torchtt)
     rounding(torchtt)
+    division(torchtt)
     small = W.small_random_system(0)
     for prec in (None, "c", "r"):
         solve_case(torchtt, cpp, small, seed=11, prec=prec, with_python=True,

@@ -134,3 +134,23 @@ def test_structured_a_matches_dense(cuda, precision):
     assert float((xs - xd).norm() / xd.norm()) <= 10 * p["eps"]
     _parity.check(A, b, [c.cpu().numpy() for c in xs.cores], G.cores(z, "x_cpp"), p["eps"],
                   p["kickrank"], label="structured " + precision)
+
+
+@pytest.mark.parametrize("fixture", ["solve_laplace_d8_n16.npz", "solve_random_4x5x6.npz"])
+def test_double_float_products_match_native(cuda, fixture):
+    """The mixed path's FP64 products in double-float arithmetic on the FP32 pipe (default) give
+    the solution of the native-FP64 products within the solve tolerance, and the reference's."""
+    from torchtt_gb300 import TT
+    from torchtt_gb300.solvers import solve_cores
+    z = G.load(fixture)
+    A, b = G.cores(z, "A"), G.cores(z, "b")
+    x0, z0 = G.cores(z, "x0"), G.cores(z, "z0")
+    p = G.params(z)
+    dev = lambda cs: [torch.from_numpy(c).to(cuda) for c in cs] if cs is not None else None
+    kw = dict(nswp=p["nswp"], eps=p["eps"], kickrank=p["kickrank"], precision="mixed",
+              preconditioner=int(z["prec"]))
+    xd, sd = solve_cores(dev(A), dev(b), dev(x0), dev(z0), fp64_engine="df", **kw)
+    xn, sn = solve_cores(dev(A), dev(b), dev(x0), dev(z0), fp64_engine="native", **kw)
+    assert float((TT(xd) - TT(xn)).norm() / TT(xn).norm()) <= 10 * p["eps"]
+    _parity.check(A, b, [c.cpu().numpy() for c in xd], G.cores(z, "x_cpp"), p["eps"],
+                  p["kickrank"], label="double-float " + fixture)

@@ -81,3 +81,24 @@ def test_round_matches_reference():
             err = O.tt_norm(O.tt_add([c.reshape(c.shape[0], -1, c.shape[-1]) for c in y],
                                      [c.reshape(c.shape[0], -1, c.shape[-1]) for c in xin], 1.0, -1.0))
             assert err <= eps * O.tt_norm(xin) * 1.0001, (name, err)
+
+
+def test_divide_by_diagonal_solve_matches_reference():
+    """Elementwise division as an AMEn solve with the diagonal TT-matrix diag(a) (the GPU path's
+    formulation), run by the oracle, reproduces the reference's amen_divide."""
+    z = G.load("divide.npz")
+    name = str(z["names"][0])
+    a, b, xr = G.cores(z, name + "_a"), G.cores(z, name + "_b"), G.cores(z, name + "_x")
+    D = []
+    for c in a:
+        r, n, R = c.shape
+        Dk = np.zeros((r, n, n, R))
+        for i in range(n):
+            Dk[:, i, i, :] = c[:, i, :]
+        D.append(Dk)
+    d = len(a)
+    rx = [1] + [2] * (d - 1) + [1]
+    x0 = [np.ones((rx[k], a[k].shape[1], rx[k + 1])) for k in range(d)]
+    x, _ = O.amen_solve(D, b, x0, nswp=22, eps=1e-10, rmax=100)
+    assert O.tt_relerr(x, xr) <= 1e-8
+    assert O.tt_relres(D, x, b) <= 1e-9

@@ -9,7 +9,8 @@ from .errors import GB300Error, IncompatibleTypes, InvalidArguments, RankMismatc
 from .tt import TT
 from . import solvers
 from .solvers import amen_solve
+from .division import amen_divide
 
-__all__ = ["TT", "amen_solve", "solvers", "errors", "GB300Error", "IncompatibleTypes",
+__all__ = ["TT", "amen_solve", "amen_divide", "solvers", "errors", "GB300Error", "IncompatibleTypes",
            "InvalidArguments", "RankMismatch", "ShapeMismatch"]
 __version__ = "0.1.0"

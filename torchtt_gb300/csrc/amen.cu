@@ -150,6 +150,7 @@ class AmenRun {
   int64_t op_count_ = 0;   // applications of the current local operator
   int64_t lowp_count_ = 0; // low-precision applications of the current local operator
   bool mixed_ = false;
+  int fp64e_ = kFp64Native;   // engine of the FP64 products (double-float on the mixed path)
   std::vector<FBuf> A32_;  // FP32 copies of the A cores (mixed path, FP32 engine)
   FBuf phil32_, phir32_, xf_, yf_, w1f_, w2f_;
   bool use_tc_ = false;    // mixed path on the tcgen05 engine
@@ -184,6 +185,7 @@ class AmenRun {
     LocalOpDims dm{rl, rA_[k], r, N_[k], N_[k], rA_[k + 1], RL, R};
     w1_.ensure(local_product_w1(dm), s_);
     w2_.ensure(local_product_w2(dm), s_);
+    Fp64EngineScope eng(fp64e_);
     if (prof_) prof_->begin();
     local_product(dm, phil, Acore(k), phir, x, y, w1_.p, w2_.p, s_, alpha, beta, &spA_[k]);
     if (prof_) prof_->end(local_product_gemm_flops(dm, &spA_[k]), 3);
@@ -194,6 +196,7 @@ class AmenRun {
   void lrhs(const double* phil, int64_t r, int k, const double* phir, int64_t R, double alpha,
             double* out) {
     wrhs_.ensure(local_rhs_workspace(rb_[k], N_[k], rb_[k + 1], r, R), s_);
+    Fp64EngineScope eng(fp64e_);
     local_rhs(rb_[k], N_[k], rb_[k + 1], r, R, phil, bcore(k), phir, alpha, out, wrhs_.p, s_);
   }
 
@@ -209,6 +212,7 @@ class AmenRun {
                                  : (double)l * N_[k] * rA_[k + 1] * R * L +
                                       a_stage * l * R * rA_[k] * N_[k] * N_[k] * rA_[k + 1] +
                                       (double)l * rA_[k] * r * N_[k] * R);
+    Fp64EngineScope eng(fp64e_);
     if (prof_) prof_->begin();
     if (fwd) {
       out = DTensor({L, rA_[k + 1], R}, s_);
@@ -225,6 +229,7 @@ class AmenRun {
              DTensor& out) {
     PhiRhsDims pd{rb_[k], rb_[k + 1], r, R, N_[k]};
     wphi_.ensure(phi_rhs_workspace(pd), s_);
+    Fp64EngineScope eng(fp64e_);
     if (fwd) {
       out = DTensor({rb_[k + 1], R}, s_);
       phi_fwd_rhs(pd, phi_in.data(), bcore(k), core, out.data(), wphi_.p, s_);
@@ -267,6 +272,7 @@ class AmenRun {
   void forward_step(int k, int swp, bool last, double& max_res);
   void z_update_forward(int k, const double* trunc);
   void setup_lowp(LocalOperator& op, int k);
+  int choose_fp64_engine();
   int rank_search_tail(const double* U, const double* SVh, int64_t a, int64_t bdim, int64_t kf,
                        const double* resvec, double norm_rhs, double thr, const LocalOperator& op,
                        int64_t nl, double* tail_buf);
@@ -281,6 +287,7 @@ void AmenRun::init(const TTView& x0, const TTView& z0) {
   if (p_.a_structure)
     for (int i = 0; i < d; ++i) spA_[i].build(Acore(i), rA_[i], N_[i], N_[i], rA_[i + 1], s_);
   mixed_ = p_.precision == 1;
+  fp64e_ = choose_fp64_engine();
   if (mixed_) {
     use_tc_ = (p_.lowp_engine == 2) || (p_.lowp_engine == 0 && tc_available());
     TTGB_REQUIRE(!use_tc_ || tc_available(), "tcgen05 engine needs an sm_100-family GPU");
@@ -520,6 +527,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
     op.phi_l = Phis_[k].data();
     op.A = Acore(k);
     op.spA = &spA_[k];
+    op.fp64_engine = fp64e_;
     op.phi_r = Phis_[k + 1].data();
     op.prec = p_.prec;
     w1_.ensure(local_product_w1(op.dims), s_);
@@ -734,6 +742,27 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
     op_count_ = 0;
     lowp_count_ = 0;
   }
+}
+
+// Double-float FP64 products need every operand inside the FP32 exponent range: the A and b cores
+// are checked here (the interfaces and solution cores are normalised by the sweep itself).
+int AmenRun::choose_fp64_engine() {
+  if (p_.fp64_engine == 1) return kFp64Native;
+  if (p_.fp64_engine == 2) return kFp64DoubleFloat;
+  if (!mixed_) return kFp64Native;
+  const int d = d_;
+  DBuf nrm((size_t)(2 * d), s_);
+  for (int i = 0; i < d; ++i) {
+    nrm2(red_, Acore(i), rA_[i] * N_[i] * N_[i] * rA_[i + 1], nrm.p + i, s_);
+    nrm2(red_, bcore(i), rb_[i] * N_[i] * rb_[i + 1], nrm.p + d + i, s_);
+  }
+  std::vector<double> h((size_t)(2 * d));
+  TTGB_CUDA(cudaMemcpyAsync(h.data(), nrm.p, 2 * d * sizeof(double), cudaMemcpyDeviceToHost, s_));
+  TTGB_CUDA(cudaStreamSynchronize(s_));
+  st_.host_syncs++;
+  for (double v : h)
+    if (!(v < 1e30) || !std::isfinite(v)) return kFp64Native;
+  return kFp64DoubleFloat;
 }
 
 // FP32 copies of the local operator for the low-precision engine (mixed path)

@@ -29,6 +29,10 @@ struct AmenParams {
   int lowp_engine = 0;         // mixed: 0 auto (tcgen05 when available), 1 FP32 CUDA cores, 2 tcgen05
   double lowp_floor = 1e-5;    // relative target of one low-precision inner solve (mixed)
   int a_structure = 1;         // 1: apply A cores of density < 1/4 from their nonzeros
+  // FP64 contractions of the local products, interfaces and local right-hand sides: 0 auto
+  // (double-float on the mixed path when A and b lie within the FP32 exponent range, native FP64
+  // otherwise), 1 native FP64, 2 double-float. QR/SVD always run in native FP64.
+  int fp64_engine = 0;
 };
 
 // A TT-matrix or TT-vector given by device pointers (borrowed).

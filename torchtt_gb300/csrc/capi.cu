@@ -128,6 +128,8 @@ AmenParams params_from_c(const ttgb_amen_params* params) {
   p.lowp_engine = params->lowp_engine;
   TTGB_REQUIRE(params->a_structure == 0 || params->a_structure == 1, "invalid a_structure");
   p.a_structure = params->a_structure;
+  TTGB_REQUIRE(params->fp64_engine >= 0 && params->fp64_engine <= 2, "invalid fp64_engine");
+  p.fp64_engine = params->fp64_engine;
   return p;
 }
 }  // namespace ttgb
@@ -151,6 +153,7 @@ void ttgb_default_params(ttgb_amen_params* p) {
   p->precision = TTGB_PRECISION_FP64;
   p->lowp_engine = 0;
   p->a_structure = 1;
+  p->fp64_engine = 0;
 }
 
 int ttgb_amen_solve(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, const ttgb_tt* z0,

@@ -8,6 +8,8 @@
 // tile leaves SMs idle.
 #include <climits>
 
+#include <type_traits>
+
 #include "contract.cuh"
 
 namespace ttgb {
@@ -141,6 +143,124 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams<T> p) {
   }
 }
 
+// The same contraction in double-float arithmetic on the FP32 pipe: every FP64 operand is split
+// into hi + lo FP32 parts (x = hi + lo to ~2^-48), a product is formed error-free from the FMA
+// residual of hi*hi plus the cross terms, and the sum is kept as an unnormalised (hi, lo) FP32 pair
+// with an error-free two-sum per step. About 10 FP32 operations per multiply-add: on GB300, where
+// the FP32 pipe is ~60x the FP64 pipe, this is several times the FP64 rate at ~1e-13 relative
+// accuracy (operands within the FP32 exponent range).
+__device__ __forceinline__ void df_split(double x, float& h, float& l) {
+  h = (float)x;
+  l = (float)(x - (double)h);
+}
+
+template <int BM, int BN>
+__global__ void __launch_bounds__(NT) contract_df_kernel(KParams<double> p) {
+  constexpr int TM = BM / 16, TN = BN / 16;
+  __shared__ float Ah[BK][BM + 1], Al[BK][BM + 1];
+  __shared__ float Bh[BK][BN + 1], Bl[BK][BN + 1];
+
+  const int tid = threadIdx.x;
+  const int bz = blockIdx.z;
+  const int bidx = bz / p.splitk;
+  const int ks = bz - bidx * p.splitk;
+  const int kbeg = ks * p.kchunk;
+  int kend = min(p.K, kbeg + p.kchunk);
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  if ((p.tri & kTriLowerC) && m0 + BM <= n0) return;
+  if (p.tri & kTriUpperB) kend = min(kend, n0 + BN);
+
+  const double* A = p.A + (int64_t)bidx * p.a_bs;
+  const double* B = p.B + (int64_t)bidx * p.b_bs;
+  constexpr int ROWS_PER_PASS = NT / BK;
+  const int lk = tid % BK;
+  const int lr = tid / BK;
+  int64_t a_moff[BM / ROWS_PER_PASS];
+  bool a_mok[BM / ROWS_PER_PASS];
+#pragma unroll
+  for (int i = 0; i < BM / ROWS_PER_PASS; ++i) {
+    const int m = m0 + lr + i * ROWS_PER_PASS;
+    a_mok[i] = m < p.M;
+    a_moff[i] = a_mok[i] ? ax_off(p.am, m) : 0;
+  }
+  int64_t b_noff[BN / ROWS_PER_PASS];
+  bool b_nok[BN / ROWS_PER_PASS];
+#pragma unroll
+  for (int i = 0; i < BN / ROWS_PER_PASS; ++i) {
+    const int n = n0 + lr + i * ROWS_PER_PASS;
+    b_nok[i] = n < p.N;
+    b_noff[i] = b_nok[i] ? ax_off(p.bn, n) : 0;
+  }
+  const int ty = tid / 16, tx = tid % 16;
+  float ch[TM][TN], cl[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) { ch[i][j] = 0.f; cl[i][j] = 0.f; }
+
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    const int k = k0 + lk;
+    const bool kok = k < kend;
+    const int64_t a_koff = kok ? ax_off(p.ak, k) : 0;
+    const int64_t b_koff = kok ? ax_off(p.bk, k) : 0;
+#pragma unroll
+    for (int i = 0; i < BM / ROWS_PER_PASS; ++i) {
+      float h, l;
+      df_split((kok && a_mok[i]) ? __ldg(A + a_moff[i] + a_koff) : 0.0, h, l);
+      Ah[lk][lr + i * ROWS_PER_PASS] = h;
+      Al[lk][lr + i * ROWS_PER_PASS] = l;
+    }
+#pragma unroll
+    for (int i = 0; i < BN / ROWS_PER_PASS; ++i) {
+      float h, l;
+      df_split((kok && b_nok[i]) ? __ldg(B + b_noff[i] + b_koff) : 0.0, h, l);
+      Bh[lk][lr + i * ROWS_PER_PASS] = h;
+      Bl[lk][lr + i * ROWS_PER_PASS] = l;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < BK; ++kk) {
+      float ah[TM], al[TM], bh[TN], bl[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) { ah[i] = Ah[kk][ty + 16 * i]; al[i] = Al[kk][ty + 16 * i]; }
+#pragma unroll
+      for (int j = 0; j < TN; ++j) { bh[j] = Bh[kk][tx + 16 * j]; bl[j] = Bl[kk][tx + 16 * j]; }
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+          const float pr = ah[i] * bh[j];
+          float e = fmaf(ah[i], bh[j], -pr);        // exact residual of the leading product
+          e = fmaf(ah[i], bl[j], e);
+          e = fmaf(al[i], bh[j], e);
+          const float s = ch[i][j] + pr;            // two-sum of the running high part and pr
+          const float bb = s - ch[i][j];
+          const float err = (ch[i][j] - (s - bb)) + (pr - bb);
+          ch[i][j] = s;
+          cl[i][j] += err + e;
+        }
+    }
+    __syncthreads();
+  }
+
+  double* C = p.C + (int64_t)bidx * p.c_bs;
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int m = m0 + ty + 16 * i;
+    if (m >= p.M) continue;
+    const int64_t cmo = ax_off(p.cm, m);
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int n = n0 + tx + 16 * j;
+      if (n >= p.N) continue;
+      double* c = C + cmo + ax_off(p.cn, n);
+      const double v = p.alpha * ((double)ch[i][j] + (double)cl[i][j]);
+      if (p.splitk > 1) atomicAdd(c, v);
+      else *c = (p.beta == 0.0) ? v : fma(p.beta, *c, v);
+    }
+  }
+}
+
 // C <- beta * C over the (batched, strided) output index space
 template <typename T>
 __global__ void scale_output_kernel(T* C, int M, int N, int batch, AxD cm, AxD cn, int64_t c_bs,
@@ -168,6 +288,8 @@ AxD to_dev(const Ax& a, int extent) {
   r.s0 = a.s0;
   return r;
 }
+
+thread_local int t_fp64_engine = kFp64Native;
 
 template <typename T>
 void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool deterministic) {
@@ -217,6 +339,16 @@ void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool determ
   }
   dim3 grid(cdiv(d.N, bn), cdiv(d.M, bm), (unsigned)(d.batch * splitk));
   TTGB_REQUIRE(grid.y < 65536 && grid.z < 65536, "contraction grid too large");
+  if constexpr (std::is_same<T, double>::value) {
+    if (t_fp64_engine == kFp64DoubleFloat) {
+      if (bm == 64 && bn == 64) contract_df_kernel<64, 64><<<grid, NT, 0, stream>>>(p);
+      else if (bm == 64 && bn == 32) contract_df_kernel<64, 32><<<grid, NT, 0, stream>>>(p);
+      else if (bm == 32 && bn == 64) contract_df_kernel<32, 64><<<grid, NT, 0, stream>>>(p);
+      else contract_df_kernel<32, 32><<<grid, NT, 0, stream>>>(p);
+      TTGB_CHECK_LAUNCH();
+      return;
+    }
+  }
   if (bm == 64 && bn == 64) contract_kernel<T, 64, 64><<<grid, NT, 0, stream>>>(p);
   else if (bm == 64 && bn == 32) contract_kernel<T, 64, 32><<<grid, NT, 0, stream>>>(p);
   else if (bm == 32 && bn == 64) contract_kernel<T, 32, 64><<<grid, NT, 0, stream>>>(p);
@@ -225,6 +357,9 @@ void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool determ
 }
 
 }  // namespace
+
+Fp64EngineScope::Fp64EngineScope(int engine) : prev_(t_fp64_engine) { t_fp64_engine = engine; }
+Fp64EngineScope::~Fp64EngineScope() { t_fp64_engine = prev_; }
 
 void contract(const ContractDesc& d, cudaStream_t stream, bool deterministic) {
   launch_contract<double>(d, stream, deterministic);

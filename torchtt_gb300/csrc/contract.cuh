@@ -42,6 +42,20 @@ constexpr int kTriUpperB = 2;
 using ContractDesc = ContractDescT<double>;
 using ContractDescF = ContractDescT<float>;
 
+// Arithmetic of the FP64 contractions issued by the calling thread: kFp64Native runs them on the
+// FP64 pipe; kFp64DoubleFloat in double-float arithmetic on the FP32 pipe (~1e-13 relative, for
+// operands within the FP32 exponent range). Set for a scope with Fp64EngineScope.
+constexpr int kFp64Native = 0;
+constexpr int kFp64DoubleFloat = 1;
+struct Fp64EngineScope {
+  explicit Fp64EngineScope(int engine);
+  ~Fp64EngineScope();
+  Fp64EngineScope(const Fp64EngineScope&) = delete;
+  Fp64EngineScope& operator=(const Fp64EngineScope&) = delete;
+ private:
+  int prev_;
+};
+
 // Launches the contraction on `stream`. Picks a split-K factor when the output has too few tiles
 // to fill the GPU (then C is pre-scaled by beta and partial sums are added atomically).
 void contract(const ContractDesc& d, cudaStream_t stream, bool deterministic = false);

@@ -26,6 +26,7 @@ void LocalOperator::apply(const double* x, double* y, bool use_prec, cudaStream_
     if (count_lowp) ++*count_lowp;
     return;
   }
+  Fp64EngineScope eng(fp64_engine);
   if (prof) prof->begin();
   local_product(dims, phi_l, A, phi_r, in, y, w1, w2, s, 1.0, 0.0, spA);
   if (prof) prof->end(local_product_gemm_flops(dims, spA), 3);
@@ -33,6 +34,7 @@ void LocalOperator::apply(const double* x, double* y, bool use_prec, cudaStream_
 }
 
 void LocalOperator::apply_fp64(const double* x, double* y, cudaStream_t s) const {
+  Fp64EngineScope eng(fp64_engine);
   if (prof) prof->begin();
   local_product(dims, phi_l, A, phi_r, x, y, w1, w2, s, 1.0, 0.0, spA);
   if (prof) prof->end(local_product_gemm_flops(dims, spA), 3);

@@ -33,6 +33,7 @@ struct LocalOperator {
   const double* A = nullptr;
   const double* phi_r = nullptr;
   const SparseCore* spA = nullptr;   // nonzero structure of A (structured A stage), optional
+  int fp64_engine = kFp64Native;     // arithmetic of the FP64 products (contract.cuh)
   int prec = kNoPrec;
   const double* J = nullptr;    // preconditioner blocks (see prec.cu)
   double* w1 = nullptr;         // local_product workspaces

@@ -51,7 +51,7 @@ def _prep(cores, device):
 def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-10, rmax=32768,
                 max_full=500, kickrank=4, kick2=0, local_iterations=40, resets=2, verbose=False,
                 preconditioner=0, seed=1, stream=None, precision="fp64", profile=False,
-                engine="auto", a_structure=True):
+                engine="auto", a_structure=True, fp64_engine="auto"):
     """Native solve on lists of CUDA float64 cores; returns ``(x_cores, stats_dict)``.
 
     This is the thin layer over ``ttgb_amen_solve`` (include/ttgb300.h); ``amen_solve`` below adds
@@ -66,7 +66,7 @@ def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-
     p = make_params(nswp=nswp, eps=eps, rmax=rmax, max_full=max_full, kickrank=kickrank,
                     kick2=kick2, local_iterations=local_iterations, resets=resets, verbose=verbose,
                     preconditioner=preconditioner, seed=seed, precision=precision, profile=profile,
-                    engine=engine, a_structure=a_structure)
+                    engine=engine, a_structure=a_structure, fp64_engine=fp64_engine)
     if stream is None:
         stream = torch.cuda.current_stream(A_cores[0].device)
     handle = _lib.c_vp()
@@ -105,9 +105,11 @@ def fetch_solution(handle, modes, device, stream):
 
 def make_params(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
                 local_iterations=40, resets=2, verbose=False, preconditioner=0, seed=1,
-                precision="fp64", profile=False, engine="auto", a_structure=True):
+                precision="fp64", profile=False, engine="auto", a_structure=True,
+                fp64_engine="auto"):
     """A ``ttgb_amen_params`` structure from keyword arguments (defaults of the reference).
-    ``a_structure=False`` forces the dense contraction of the A cores."""
+    ``a_structure=False`` forces the dense contraction of the A cores; ``fp64_engine`` is
+    'auto' (double-float FP64 products on the mixed path), 'native' or 'df'."""
     p = _lib.AmenParams()
     _lib.lib().ttgb_default_params(ctypes.byref(p))
     p.nswp, p.eps, p.rmax, p.max_full = int(nswp), float(eps), int(rmax), int(max_full)
@@ -123,6 +125,10 @@ def make_params(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=
         raise InvalidArguments("engine must be 'auto', 'fp32' or 'tc'")
     p.lowp_engine = engines[engine]
     p.a_structure = int(bool(a_structure))
+    engines64 = {"auto": 0, "native": 1, "df": 2}
+    if fp64_engine not in engines64:
+        raise InvalidArguments("fp64_engine must be 'auto', 'native' or 'df'")
+    p.fp64_engine = engines64[fp64_engine]
     return p
 
 

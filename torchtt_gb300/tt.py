@@ -137,6 +137,27 @@ class TT:
 
     __rmul__ = __mul__
 
+    def __truediv__(self, other):
+        """``self / other``: by a scalar, or elementwise by a TT of the same shape through AMEn on
+        the GPU with the reference's fixed settings (50 sweeps, eps 1e-12, rmax 500;
+        torchtt/_tt_base.py:900-934)."""
+        if isinstance(other, (int, float)) or (torch.is_tensor(other) and other.numel() == 1):
+            return TT([self.cores[0] / other] + self.cores[1:])
+        if isinstance(other, TT) or (hasattr(other, "cores") and hasattr(other, "is_ttm")):
+            from .division import amen_divide
+            return TT(amen_divide(other, self, 50, None, 1e-12, 500))
+        raise InvalidArguments("Operand not permitted. A TT-object can be divided only with scalars.")
+
+    def __rtruediv__(self, other):
+        """``scalar / self`` elementwise through AMEn on the GPU (torchtt/_tt_base.py:936-966)."""
+        if isinstance(other, (int, float)) or (torch.is_tensor(other) and other.numel() == 1):
+            from .division import amen_divide
+            ones = TT([torch.ones((1,) + tuple(c.shape[1:-1]) + (1,), dtype=c.dtype, device=c.device)
+                       for c in self.cores])
+            ones.cores[0] = ones.cores[0] * other
+            return TT(amen_divide(self, ones, 50, None, 1e-12, 500))
+        raise InvalidArguments("The first operand must be int, float or 1d torch.tensor.")
+
     def _device_cores(self):
         """The cores as contiguous CUDA float64 tensors (copied to the current GPU if needed)."""
         if not torch.cuda.is_available():
