@@ -161,6 +161,12 @@ void ttgb_server_destroy(ttgb_server* srv);
 /* y = A x for a TT-matrix A and a TT-vector x (ranks multiply); the result is a library-owned
    ttgb_solution. (replaces TT.__matmul__, torchtt/_tt_base.py:807-817) */
 int ttgb_tt_matvec(const ttgb_tt* A, const ttgb_tt* x, void* stream, ttgb_solution** out);
+/* y ~ A x by two-site DMRG to relative accuracy eps (replaces dmrg_mv, cpp/dmrg_mv.h:23-230,
+   torchttcpp.dmrg_mv / torchtt dmrg_matvec, torchtt/_dmrg.py:22-45). y0 may be NULL (random start
+   of rank 2 from `seed`); the result is a library-owned ttgb_solution. */
+int ttgb_dmrg_matvec(const ttgb_tt* A, const ttgb_tt* x, const ttgb_tt* y0, int32_t nswp,
+                     double eps, int64_t rmax, int32_t kickrank, uint64_t seed, int32_t verbose,
+                     void* stream, ttgb_solution** out);
 /* ||x||_F by a QR sweep (replaces TT.norm, torchtt/_tt_base.py:1021-1051). */
 int ttgb_tt_norm(const ttgb_tt* x, double* out, void* stream);
 /* TT rounding to relative accuracy eps with rank cap rmax; the result is a library-owned

@@ -575,3 +575,101 @@ def tt_round(cores, eps, rmax=2 ** 62):
         prev = cs[i - 1]
         cs[i - 1] = (prev.reshape(-1, r) @ (u[:, :rn] * s[:rn])).reshape(prev.shape[0], prev.shape[1], rn)
     return [c.reshape((c.shape[0],) + tuple(sh[1:-1]) + (c.shape[-1],)) for c, sh in zip(cs, shapes)]
+
+
+# --------------------------------------------------------------------------------------------------
+# DMRG matvec (cpp/dmrg_mv.h:23-230)
+# --------------------------------------------------------------------------------------------------
+
+def _rank_chop_cpp(s, tol):
+    """rank_chop of cpp/ortho.h:16-45 (the C++ DMRG uses it): largest r with a discarded tail
+    sum_{k >= r} s_k^2 >= tol^2, plus one; 1 for s = 0."""
+    s = np.asarray(s)
+    n = s.size
+    if np.linalg.norm(s) == 0.0:
+        return 1
+    if tol <= 0.0:
+        return n - 1
+    r = n - 1
+    while r > 0:
+        if np.sum(s[r:] ** 2) >= tol * tol:
+            break
+        r -= 1
+    return max(r + 1, 1)
+
+
+def dmrg_matvec(A_cores, x_cores, y0_cores=None, nswp=20, eps=1e-12, rmax=32768, kickrank=4,
+                rng=None):
+    """y ~ A x by two-site DMRG, restating dmrg_mv (cpp/dmrg_mv.h:23-230) step by step: a
+    right-to-left QR sweep with backward interfaces, then two-site blocks truncated by SVD with
+    rank_chop at eps ||W|| / d^1.5 (d^0.5 in the last sweep) plus an adaptive enlargement, and
+    kickrank random directions. Random numbers come from `rng` (a numpy Generator)."""
+    rng = rng if rng is not None else np.random.default_rng(0)
+    d = len(A_cores)
+    M = [a.shape[1] for a in A_cores]
+    if y0_cores is None:
+        ry = [1] + [2] * (d - 1) + [1]
+        y = [rng.standard_normal((ry[k], M[k], ry[k + 1])) for k in range(d)]
+    else:
+        y = [c.copy() for c in y0_cores]
+        ry = [1] + [c.shape[2] for c in y]
+    Phis = [np.ones((1, 1, 1))] + [None] * (d - 1) + [np.ones((1, 1, 1))]
+    delta = np.ones(d - 1)
+    delta_prev = np.ones(d - 1)
+    renl = [2] * d
+    last = False
+    for swp in range(nswp):
+        for k in range(d - 1, 0, -1):
+            core = y[k].transpose(1, 2, 0).reshape(M[k] * ry[k + 1], ry[k])
+            Q, R = np.linalg.qr(core)
+            rnew = min(core.shape)
+            y[k] = Q.T.reshape(rnew, M[k], -1)
+            ry[k] = rnew
+            y[k - 1] = np.tensordot(y[k - 1].reshape(-1, y[k - 1].shape[2]), R, axes=([1], [1])).reshape(-1, M[k - 1], rnew)
+            Phi = np.tensordot(Phis[k + 1], x_cores[k], axes=([2], [2]))
+            Phi = np.tensordot(A_cores[k], Phi, axes=([2, 3], [3, 1]))
+            Phis[k] = np.tensordot(y[k], Phi, axes=([1, 2], [1, 2]))
+        for k in range(d - 1):
+            W_prev = np.tensordot(y[k], y[k + 1], axes=([2], [0]))
+            if not last:
+                W1 = np.tensordot(Phis[k], x_cores[k], axes=([2], [0]))
+                W1 = np.tensordot(A_cores[k], W1, axes=([0, 2], [1, 2]))
+                W2 = np.tensordot(Phis[k + 2], x_cores[k + 1], axes=([2], [2]))
+                W2 = np.tensordot(A_cores[k + 1], W2, axes=([2, 3], [3, 1]))
+                W = np.tensordot(W1, W2, axes=([1, 3], [0, 3])).transpose(1, 0, 2, 3)
+            else:
+                W = W_prev
+            b = np.linalg.norm(W)
+            delta[k] = np.linalg.norm(W - W_prev) / b if b > 0 else 0.0
+            with np.errstate(divide="ignore", invalid="ignore"):
+                ratio = delta[k] / delta_prev[k]
+            if ratio >= 1 and delta[k] > eps:
+                renl[k] += 1
+            if ratio < 0.1 and delta[k] < eps:
+                renl[k] = max(renl[k] - 1, 1)
+            U, S, V = np.linalg.svd(W.reshape(W.shape[0] * W.shape[1], -1), full_matrices=False)
+            r_new = _rank_chop_cpp(S, b * eps / d ** (0.5 if last else 1.5))
+            if not last:
+                r_new += renl[k]
+            r_new = max(min(r_new, S.size, rmax), 1)
+            W1 = U[:, :r_new]
+            W2 = V[:r_new, :].T * S[:r_new]
+            if swp < nswp - 1:
+                W1, Rm = np.linalg.qr(np.concatenate([W1, rng.standard_normal((W1.shape[0], kickrank))], 1))
+                W2 = np.concatenate([W2, np.zeros((W2.shape[0], kickrank))], 1)
+                W2 = np.tensordot(Rm, W2, axes=([1], [1]))
+                r_new = W1.shape[1]
+            else:
+                W2 = W2.T
+            ry[k + 1] = r_new
+            y[k] = W1.reshape(ry[k], M[k], r_new)
+            y[k + 1] = W2.reshape(r_new, M[k + 1], ry[k + 2])
+            Pn = np.tensordot(Phis[k], x_cores[k], axes=([2], [0]))
+            Pn = np.tensordot(Pn, A_cores[k], axes=([1, 2], [0, 2]))
+            Phis[k + 1] = np.tensordot(y[k], Pn, axes=([0, 1], [0, 2])).transpose(0, 2, 1)
+        if last:
+            break
+        if delta.max() < eps:
+            last = True
+        delta_prev = delta.copy()
+    return y

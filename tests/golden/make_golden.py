@@ -10,6 +10,7 @@ Python package is imported from the tree. Writes ``tests/golden/*.npz``:
   1-D Laplacian, the pattern of ``cpp/test_gmres.cpp:187-253``);
 * ``round.npz`` - inputs and outputs of the reference's TT rounding (``TT.round``);
 * ``divide.npz`` - inputs and outputs of the reference's elementwise division (``amen_divide``);
+* ``dmrg.npz`` - inputs and outputs of the reference's C++ DMRG matvec (``dmrg_mv``);
 * ``solve_<name>.npz`` - the inputs of a whole solve (A, b, x0 cores, the initial enrichment cores z0
   that the reference drew with ``torch::randn`` after ``torch.manual_seed``), the parameters, and the
   solution cores returned by ``torchttcpp.amen_solve`` (``cpp/amen_solve.h:122``) and, for the small
@@ -138,6 +139,25 @@ def division(torchtt):
     print("divide.npz written")
 
 
+def dmrg(cpp):
+    """The reference's C++ DMRG matvec (torchttcpp.dmrg_mv, cpp/dmrg_mv.h:23) on a Laplacian and a
+    Laplacian-plus-potential operator; the random start and kicks come from the global torch RNG
+    (seeded here, not replayable elsewhere), so parity is on the product."""
+    out = {}
+    cases = [("lap", W.laplace_ttm(5, 6), [6] * 5, [1, 3, 3, 3, 3, 1], 21),
+             ("pot", W.laplace_potential_ttm(4, 8), [8] * 4, [1, 4, 4, 4, 1], 22)]
+    for name, A, N, R, seed in cases:
+        x = W.random_tt(N, R, seed)
+        torch.manual_seed(seed)
+        y = cpp.dmrg_mv(A, x, [], N, N, R, [], 20, 1e-12, 32768, 4, False)
+        _pack_cores(name + "_A", A, out)
+        _pack_cores(name + "_x", x, out)
+        _pack_cores(name + "_y", y, out)
+    out["names"] = np.array([c[0] for c in cases])
+    np.savez_compressed(os.path.join(HERE, "dmrg.npz"), **out)
+    print("dmrg.npz written")
+
+
 def solve_case(torchtt, cpp, wl, seed, prec=None, with_python=False, extra=None):
     A, b, x0 = wl["A"], wl["b"], wl.get("x0")
     p = dict(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
@@ -191,6 +211,7 @@ def main():
     kernels(torchtt)
     rounding(torchtt)
     division(torchtt)
+    dmrg(cpp)
     small = W.small_random_system(0)
     for prec in (None, "c", "r"):
         solve_case(torchtt, cpp, small, seed=11, prec=prec, with_python=True,

@@ -102,3 +102,16 @@ def test_divide_by_diagonal_solve_matches_reference():
     x, _ = O.amen_solve(D, b, x0, nswp=22, eps=1e-10, rmax=100)
     assert O.tt_relerr(x, xr) <= 1e-8
     assert O.tt_relres(D, x, b) <= 1e-9
+
+
+def test_dmrg_matvec_matches_reference():
+    """The oracle's DMRG matvec against the reference's C++ dmrg_mv: the same ranks, the same
+    product to ~1e-14 (both approximate A x to eps 1e-12)."""
+    z = G.load("dmrg.npz")
+    for name in z["names"]:
+        name = str(name)
+        A, x, yr = G.cores(z, name + "_A"), G.cores(z, name + "_x"), G.cores(z, name + "_y")
+        y = O.dmrg_matvec(A, x, eps=1e-12)
+        assert [c.shape for c in y] == [c.shape for c in yr], name
+        assert O.tt_relerr(y, yr) <= 1e-12
+        assert O.tt_relerr(y, O.tt_matvec(A, x)) <= 1e-12

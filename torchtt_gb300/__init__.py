@@ -10,7 +10,8 @@ from .tt import TT
 from . import solvers
 from .solvers import amen_solve
 from .division import amen_divide
+from .dmrg import dmrg_matvec
 
-__all__ = ["TT", "amen_solve", "amen_divide", "solvers", "errors", "GB300Error", "IncompatibleTypes",
+__all__ = ["TT", "amen_solve", "amen_divide", "dmrg_matvec", "solvers", "errors", "GB300Error", "IncompatibleTypes",
            "InvalidArguments", "RankMismatch", "ShapeMismatch"]
 __version__ = "0.1.0"

@@ -15,6 +15,7 @@
 #include "tc_gemm.cuh"
 #include "tc_local.cuh"
 #include "tt_ops.cuh"
+#include "dmrg.cuh"
 
 using namespace ttgb;
 
@@ -240,6 +241,27 @@ int ttgb_tt_matvec(const ttgb_tt* A, const ttgb_tt* x, void* stream, ttgb_soluti
     std::unique_ptr<ttgb_solution> sol(new ttgb_solution());
     sol->res.cores = tt_matvec(va, vx, s, sol->res.ranks);
     TTGB_CUDA(cudaStreamSynchronize(s));
+    *out = sol.release();
+  });
+}
+
+int ttgb_dmrg_matvec(const ttgb_tt* A, const ttgb_tt* x, const ttgb_tt* y0, int32_t nswp,
+                     double eps, int64_t rmax, int32_t kickrank, uint64_t seed, int32_t verbose,
+                     void* stream, ttgb_solution** out) {
+  return guarded([&] {
+    TTGB_REQUIRE(A && x && out && A->d > 0 && A->d == x->d, "bad DMRG arguments");
+    TTGB_REQUIRE(A->rows != nullptr && x->rows == nullptr,
+                 "A must be a TT-matrix and x a TT-vector.");
+    const TTView va = view_of(A, true), vx = view_of(x, false), vy = view_of(y0, false);
+    DmrgParams p;
+    p.nswp = nswp; p.eps = eps; p.rmax = rmax; p.kickrank = kickrank; p.seed = seed;
+    p.verbose = verbose;
+    Scratch sc(as_stream(stream));
+    std::unique_ptr<ttgb_solution> sol(new ttgb_solution());
+    DmrgStats st;
+    sol->res.cores = dmrg_matvec(va, vx, vy, p, sc.s, sol->res.ranks, &st, sc.lws, sc.red);
+    sol->res.stats.sweeps = st.sweeps;
+    sol->res.stats.max_res = st.max_delta;
     *out = sol.release();
   });
 }

@@ -28,7 +28,8 @@ sparse_stage_kernel(const int* __restrict__ rp, const int* __restrict__ ja,
   }
   __syncthreads();
   const int64_t total = g.O1 * g.O2;
-  T* ob = out + (int64_t)key * g.sk;
+  const int64_t koff = g.ke0 > 0 ? (key % g.ke0) * g.sk + (key / g.ke0) * g.sk1 : (int64_t)key * g.sk;
+  T* ob = out + koff;
   for (int64_t t = (int64_t)blockIdx.y * blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.y * blockDim.x) {
     const int64_t o1 = t / g.O2, o2 = t - o1 * g.O2;
@@ -39,7 +40,7 @@ sparse_stage_kernel(const int* __restrict__ rp, const int* __restrict__ ja,
     if constexpr (SPLIT) {
       const float h = to_tf32((float)acc);
       ob[o] = h;
-      out_lo[(int64_t)key * g.sk + o] = to_tf32((float)acc - h);
+      out_lo[koff + o] = to_tf32((float)acc - h);
     } else {
       ob[o] = acc;
     }
@@ -119,7 +120,7 @@ void SparseCore::build(const double* A, int64_t s_, int64_t M_, int64_t N_, int6
   std::vector<double> h(ne);
   TTGB_CUDA(cudaMemcpyAsync(h.data(), A, ne * sizeof(double), cudaMemcpyDeviceToHost, st));
   TTGB_CUDA(cudaStreamSynchronize(st));
-  std::vector<Entry> elp, efw, ebk;
+  std::vector<Entry> elp, efw, ebk, erh;
   for (int64_t a = 0; a < s; ++a)
     for (int64_t m = 0; m < M; ++m)
       for (int64_t n = 0; n < N; ++n)
@@ -129,13 +130,16 @@ void SparseCore::build(const double* A, int64_t s_, int64_t M_, int64_t N_, int6
           elp.push_back({m * S + b, (int)a, (int)n, v});
           efw.push_back({n * S + b, (int)a, (int)m, v});
           ebk.push_back({a * N + n, (int)m, (int)b, v});
+          erh.push_back({a * M + m, (int)n, (int)b, v});
         }
   const int64_t nnz = (int64_t)elp.size();
   if (4 * nnz >= ne) return;   // dense enough for the GEMM path
   upload(lp, elp, M * S, st);
   upload(fw, efw, N * S, st);
   upload(bk, ebk, s * N, st);
-  use = lp.max_row <= kMaxRow && fw.max_row <= kMaxRow && bk.max_row <= kMaxRow;
+  upload(rh, erh, s * M, st);
+  use = lp.max_row <= kMaxRow && fw.max_row <= kMaxRow && bk.max_row <= kMaxRow &&
+        rh.max_row <= kMaxRow;
 }
 
 void sparse_stage(const SparseCsr& c, const double* in, double* out, const StageDims& g,

@@ -29,16 +29,19 @@ struct SparseCore {
   SparseCsr lp;   // key (m, S) = m*S + S, pairs (s, n): local product stage
   SparseCsr fw;   // key (N, S) = N*S + S, pairs (s, M): forward interface stage
   SparseCsr bk;   // key (s, N) = s*N + N, pairs (M, S): backward interface stage
+  SparseCsr rh;   // key (s, M) = s*M + M, pairs (N, S): right half of a two-site product
   // Reads the core (device, FP64, s x M x N x S) once and sets `use` when fewer than a quarter of
   // its entries are nonzero and no key has more than kMaxRow nonzeros.
   void build(const double* A, int64_t s, int64_t M, int64_t N, int64_t S, cudaStream_t st);
   static constexpr int kMaxRow = 64;
 };
 
-// out[key*sk + o1*so1 + o2] = sum_{j in row key} val[j] * in[o1*si1 + o2 + a[j]*pa + b[j]*pb]
-// for every key < c.keys, o1 < O1, o2 < O2 (the output is overwritten).
+// out[koff(key) + o1*so1 + o2] = sum_{j in row key} val[j] * in[o1*si1 + o2 + a[j]*pa + b[j]*pb]
+// for every key < c.keys, o1 < O1, o2 < O2 (the output is overwritten), where
+// koff(key) = key*sk, or (key % ke0)*sk + (key / ke0)*sk1 when ke0 > 0.
 struct StageDims {
   int64_t O1, O2, si1, so1, sk, pa, pb;
+  int64_t ke0 = 0, sk1 = 0;
 };
 void sparse_stage(const SparseCsr& c, const double* in, double* out, const StageDims& g,
                   cudaStream_t s);
