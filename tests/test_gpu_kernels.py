@@ -97,7 +97,8 @@ def test_qr_rank_deficient(cuda):
     assert np.linalg.norm(q @ r - a) <= 1e-12 * np.linalg.norm(a)
 
 
-@pytest.mark.parametrize("mn", [(3840, 68), (512, 8), (8, 512), (70, 70), (1000, 30)])
+@pytest.mark.parametrize("mn", [(3840, 68), (512, 8), (8, 512), (70, 70), (1000, 30), (2000, 200),
+                                (700, 700)])
 def test_svd(cuda, mn):
     from torchtt_gb300 import ops
     m, n = mn

@@ -185,7 +185,41 @@ std::vector<DTensor> dmrg_matvec(const TTView& A, const TTView& x, const TTView&
       // W = Vh^T S U^T, left factor Vh^T (p1 x kk), right factor S U^T (kk x q2)
       const int64_t kk = std::min(p1, q2);
       DBuf U((size_t)(q2 * kk), s), Sv((size_t)kk, s), Vh((size_t)(kk * p1), s);
-      svd(W.p, q2, q2, p1, U.p, Sv.p, Vh.p, ws, red, s);
+      // W = F1 F2^T with a small inner dimension K: outside the last sweep F1 = Y2 (p1 x K, the
+      // local product's intermediate in w2) and F2 = Psi (q2 x K), K = rA_{k+1} rx_{k+1}; in the
+      // last sweep W = y_k y_{k+1}, K = ry_{k+1}. Then W = Q_L (R_L R_R^T) Q_R^T from the QRs of the
+      // two tall factors and the SVD of the small K x K core: the singular triplets of W.
+      const int64_t K = last ? ry[k + 1] : rA[k + 1] * rx[k + 1];
+      if (K < kk) {
+        DBuf Lc((size_t)(p1 * K), s), Rc;
+        const double* F2cm = nullptr;   // F2 in column-major (q2 x K, ld q2)
+        if (last) {
+          transpose(y[k].data(), K, Lc.p, p1, K, p1, s);   // y_k (p1 x K row-major) -> column-major
+          F2cm = y[k + 1].data();                         // y_{k+1} (K x q2 row-major) == F2 column-major
+        } else {
+          transpose(w2.p, K, Lc.p, p1, K, p1, s);         // Y2 (p1 x K row-major) -> column-major
+          Rc.reset((size_t)(q2 * K), s);
+          transpose(Psi.p, K, Rc.p, q2, K, q2, s);        // Psi (q2 x K row-major) -> column-major
+          F2cm = Rc.p;
+        }
+        DBuf QL((size_t)(p1 * K), s), RL((size_t)(K * K), s), QR_((size_t)(q2 * K), s), RR((size_t)(K * K), s);
+        qr(Lc.p, p1, p1, K, QL.p, RL.p, ws, red, s);
+        qr(F2cm, q2, q2, K, QR_.p, RR.p, ws, red, s);
+        DBuf Cc((size_t)(K * K), s), Uc((size_t)(K * K), s), Sc((size_t)K, s), Vc((size_t)(K * K), s);
+        gemm_cm(RL.p, K, RR.p, K, Cc.p, K, K, K, K, 1.0, 0.0, s, false, true);   // R_L R_R^T
+        svd(Cc.p, K, K, K, Uc.p, Sc.p, Vc.p, ws, red, s);
+        // right singular vectors Q_R Vc^T (q2 x K) -> U[:, :K]; left Q_L Uc (p1 x K) -> Vh[:K, :]
+        gemm_cm(QR_.p, q2, Vc.p, K, U.p, q2, q2, K, K, 1.0, 0.0, s, false, true);
+        DBuf Lf((size_t)(p1 * K), s);
+        gemm_cm(QL.p, p1, Uc.p, K, Lf.p, p1, p1, K, K, 1.0, 0.0, s);
+        fill(Vh.p, 0.0, kk * p1, s);
+        fill(Sv.p, 0.0, kk, s);
+        transpose(Lf.p, p1, Vh.p, kk, p1, K, s);            // Vh (kk x p1, ld kk) rows 0..K-1
+        copy(Sc.p, Sv.p, K, s);
+        fill(U.p + q2 * K, 0.0, q2 * (kk - K), s);
+      } else {
+        svd(W.p, q2, q2, p1, U.p, Sv.p, Vh.p, ws, red, s);
+      }
       hs.resize(kk);
       TTGB_CUDA(cudaMemcpyAsync(hs.data(), Sv.p, kk * sizeof(double), cudaMemcpyDeviceToHost, s));
       TTGB_CUDA(cudaStreamSynchronize(s));

@@ -536,115 +536,30 @@ __global__ void __launch_bounds__(512) jacobi_svd_kernel(double* Wg, double* Vg,
 }
 
 // ---------------------------------------------------------------------------------------------
-// One-sided Jacobi on a thread-block cluster: the FP64 work of a sweep is spread over
-// kJacobiCluster SMs. Column j of W and of V lives in the shared memory of CTA j % C (slot j / C);
-// in every round of the round-robin ordering each CTA's warps rotate their share of the n/2
-// disjoint pairs, reading and writing partner columns through distributed shared memory, and one
-// cluster barrier separates rounds. The sweep count is summed in CTA 0 after a barrier and read by
-// every CTA after another, so all CTAs leave the loop together.
+// Block one-sided Jacobi on a thread-block cluster of kJacobiCluster CTAs for 16 <= n <=
+// kJacobiBlockMaxN: the columns (padded to P = 2C blocks of nb) are treated as P blocks paired by
+// the round-robin tournament; in round r the CTA i holds the blocks rr(i, r) and rr(P-1-i, r) in its
+// own shared memory and rotates all their cross pairs there (nb sub-rounds of nb disjoint pairs,
+// block barrier only; the pairs inside a block are rotated in the first round of each sweep), then
+// pulls the two blocks of its next pair from their holders over DSMEM into its second buffer. Every
+// pair of columns is visited once per sweep, as in the scalar cyclic order, with one cluster
+// barrier per round (P - 1 per sweep), and every dot product reads local memory. The sweep's
+// rotation count is summed in CTA 0 after a barrier and read by every CTA, so all CTAs leave the
+// loop together.
 // ---------------------------------------------------------------------------------------------
 constexpr int kJacobiCluster = 8;
-constexpr int kJacobiClusterMaxN = 320;   // 2 ceil(n/8) n doubles of shared memory per CTA
-
-__global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
-    jacobi_cluster_kernel(const double* __restrict__ Win, int n, double* Wout, double* Vout,
-                          int max_sweeps, int* status) {
-  extern __shared__ double sm[];
-  cg::cluster_group cluster = cg::this_cluster();
-  const int C = kJacobiCluster;
-  const int rank = (int)cluster.block_rank();
-  const int ncl = (n + C - 1) / C;
-  double* Wl = sm;
-  double* Vl = sm + (int64_t)ncl * n;
-  __shared__ int counts[kJacobiCluster];   // CTA 0's copy collects the per-CTA rotation counts
-  __shared__ int local_cnt;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  for (int t = 0; t < ncl; ++t) {
-    const int j = rank + C * t;
-    for (int i = tid; i < n; i += nt) {
-      Wl[(int64_t)t * n + i] = (j < n) ? Win[(int64_t)j * n + i] : 0.0;
-      Vl[(int64_t)t * n + i] = (j < n && i == j) ? 1.0 : 0.0;
-    }
-  }
-  int* counts0 = cluster.map_shared_rank(counts, 0);
-  const int nn = n + (n & 1);
-  const double tol = fmax((double)n, 1.0) * kEps;
-  int sweep = 0;
-  bool converged = false;
-  for (; sweep < max_sweeps; ++sweep) {
-    if (tid == 0) local_cnt = 0;
-    cluster.sync();
-    int mine = 0;
-    for (int r = 0; r < nn - 1; ++r) {
-      for (int pi = rank + C * warp; pi < nn / 2; pi += C * nw) {
-        int p = rr_index(pi, r, nn), q = rr_index(nn - 1 - pi, r, nn);
-        if (p > q) { const int t = p; p = q; q = t; }
-        if (q >= n) continue;
-        double* wp = cluster.map_shared_rank(Wl + (int64_t)(p / C) * n, p % C);
-        double* wq = cluster.map_shared_rank(Wl + (int64_t)(q / C) * n, q % C);
-        double a = 0.0, b = 0.0, g = 0.0;
-        for (int i = lane; i < n; i += 32) {
-          const double x = wp[i], y = wq[i];
-          a = fma(x, x, a); b = fma(y, y, b); g = fma(x, y, g);
-        }
-        a = warp_sum_d(a); b = warp_sum_d(b); g = warp_sum_d(g);
-        double c, s;
-        if (!jacobi_rotation(a, b, g, tol, c, s)) continue;
-        for (int i = lane; i < n; i += 32) {
-          const double x = wp[i], y = wq[i];
-          wp[i] = c * x - s * y;
-          wq[i] = s * x + c * y;
-        }
-        double* vp = cluster.map_shared_rank(Vl + (int64_t)(p / C) * n, p % C);
-        double* vq = cluster.map_shared_rank(Vl + (int64_t)(q / C) * n, q % C);
-        for (int i = lane; i < n; i += 32) {
-          const double x = vp[i], y = vq[i];
-          vp[i] = c * x - s * y;
-          vq[i] = s * x + c * y;
-        }
-        ++mine;
-      }
-      cluster.sync();
-    }
-    if (lane == 0 && mine) atomicAdd(&local_cnt, mine);
-    __syncthreads();
-    if (tid == 0) counts0[rank] = local_cnt;
-    cluster.sync();
-    int total = 0;
-    for (int c = 0; c < C; ++c) total += counts0[c];
-    cluster.sync();
-    if (total == 0) { converged = true; break; }
-  }
-  if (rank == 0 && tid == 0 && !converged) *status = 3;
-  for (int t = 0; t < ncl; ++t) {
-    const int j = rank + C * t;
-    if (j >= n) break;
-    for (int i = tid; i < n; i += nt) {
-      Wout[(int64_t)j * n + i] = Wl[(int64_t)t * n + i];
-      Vout[(int64_t)j * n + i] = Vl[(int64_t)t * n + i];
-    }
-  }
-}
-
-// Block variant of the cluster Jacobi for 16 <= n <= kJacobiBlockMaxN: the columns (padded to
-// P = 2C blocks of nb) are treated as P blocks paired by the round-robin tournament; in round r the
-// CTA i holds the blocks rr(i, r) and rr(P-1-i, r) in its own shared memory and rotates all their
-// cross pairs there (nb sub-rounds of nb disjoint pairs, block barrier only; the pairs inside a
-// block are rotated in the first round of each sweep), then pulls the two blocks of its next
-// pair from their holders over DSMEM into its second buffer. Every pair of columns is visited once
-// per sweep, as in the scalar cyclic order, with one cluster barrier per round (P - 1 per sweep)
-// instead of one per pair round (n - 1 per sweep), and every dot product reads local memory.
 constexpr int kJacobiBlockMaxN = 160;
 
-__device__ __forceinline__ int jacobi_rotate_pair(double* wp, double* wq, double* vp, double* vq,
-                                                  int n, double tol, int lane) {
-  double a = 0.0, b = 0.0, g = 0.0;
-  for (int i = lane; i < n; i += 32) {
-    const double x = wp[i], y = wq[i];
-    a = fma(x, x, a); b = fma(y, y, b); g = fma(x, y, g);
-  }
-  a = warp_sum_d(a); b = warp_sum_d(b); g = warp_sum_d(g);
+// One rotation of a column pair with tracked squared column norms (*na, *nb): only the inner product is
+// reduced; the norms follow the rotation exactly (a' = c^2 a - 2cs g + s^2 b, b' = s^2 a + 2cs g +
+// c^2 b) and are recomputed from the columns once per sweep, which bounds their drift.
+__device__ __forceinline__ int jacobi_rotate_tracked(double* wp, double* wq, double* vp, double* vq,
+                                                     double* na, double* nb, int n, double tol,
+                                                     int lane) {
+  double g = 0.0;
+  for (int i = lane; i < n; i += 32) g = fma(wp[i], wq[i], g);
+  g = warp_sum_d(g);
+  const double a = *na, b = *nb;
   double c, s;
   if (!jacobi_rotation(a, b, g, tol, c, s)) return 0;
   for (int i = lane; i < n; i += 32) {
@@ -654,6 +569,11 @@ __device__ __forceinline__ int jacobi_rotate_pair(double* wp, double* wq, double
     const double u = vp[i], v = vq[i];
     vp[i] = c * u - s * v;
     vq[i] = s * u + c * v;
+  }
+  if (lane == 0) {
+    const double cc = c * c, ss = s * s, cs2 = 2.0 * c * s * g;
+    *na = fmax(cc * a - cs2 + ss * b, 0.0);
+    *nb = fmax(ss * a + cs2 + cc * b, 0.0);
   }
   return 1;
 }
@@ -667,9 +587,11 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
   const int rank = (int)cluster.block_rank();
   const int nb = (n + P - 1) / P;
   const int64_t blk = (int64_t)nb * n;   // doubles of one block of W (or of V)
-  // buffer x (0/1), slot s (0/1): W block then V block
-  auto Wb = [&](double* base, int x, int sl) { return base + ((int64_t)(x * 2 + sl) * 2) * blk; };
-  auto Vb = [&](double* base, int x, int sl) { return base + ((int64_t)(x * 2 + sl) * 2 + 1) * blk; };
+  const int64_t unit = 2 * blk + nb + (nb & 1);   // W block, V block, squared column norms
+  // buffer x (0/1), slot s (0/1): W block, V block, norms
+  auto Wb = [&](double* base, int x, int sl) { return base + (int64_t)(x * 2 + sl) * unit; };
+  auto Vb = [&](double* base, int x, int sl) { return base + (int64_t)(x * 2 + sl) * unit + blk; };
+  auto Nb = [&](double* base, int x, int sl) { return base + (int64_t)(x * 2 + sl) * unit + 2 * blk; };
   __shared__ int counts[kJacobiCluster];
   __shared__ int local_cnt;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -694,9 +616,17 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
   __syncthreads();
   while (true) {
     const int bA = rr_index(rank, r, P), bB = rr_index(P - 1 - rank, r, P);
-    double* WA = Wb(sm, x, 0); double* VA = Vb(sm, x, 0);
-    double* WB = Wb(sm, x, 1); double* VB = Vb(sm, x, 1);
-    if (r == 0) {   // pairs inside each block, once per sweep
+    double* WA = Wb(sm, x, 0); double* VA = Vb(sm, x, 0); double* NA = Nb(sm, x, 0);
+    double* WB = Wb(sm, x, 1); double* VB = Vb(sm, x, 1); double* NB = Nb(sm, x, 1);
+    if (r == 0) {   // fresh column norms, then the pairs inside each block, once per sweep
+      for (int c = warp; c < 2 * nb; c += nw) {
+        const double* w = (c < nb ? WA : WB) + (int64_t)(c % nb) * n;
+        double a = 0.0;
+        for (int i = lane; i < n; i += 32) a = fma(w[i], w[i], a);
+        a = warp_sum_d(a);
+        if (lane == 0) (c < nb ? NA : NB)[c % nb] = a;
+      }
+      __syncthreads();
       const int m2 = nb + (nb & 1);
       for (int t = 0; t < m2 - 1; ++t) {
         for (int task = warp; task < m2; task += nw) {   // m2/2 pairs per slot, 2 slots
@@ -706,8 +636,9 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
           if (q >= nb) continue;
           double* W = sl ? WB : WA;
           double* V = sl ? VB : VA;
-          mine += jacobi_rotate_pair(W + (int64_t)p * n, W + (int64_t)q * n, V + (int64_t)p * n,
-                                     V + (int64_t)q * n, n, tol, lane);
+          double* Nm = sl ? NB : NA;
+          mine += jacobi_rotate_tracked(W + (int64_t)p * n, W + (int64_t)q * n, V + (int64_t)p * n,
+                                        V + (int64_t)q * n, Nm + p, Nm + q, n, tol, lane);
         }
         __syncthreads();
       }
@@ -718,8 +649,11 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
         const int ga = bA * nb + j, gb = bB * nb + k;
         double *wp = WA + (int64_t)j * n, *wq = WB + (int64_t)k * n;
         double *vp = VA + (int64_t)j * n, *vq = VB + (int64_t)k * n;
-        if (ga > gb) { double* u = wp; wp = wq; wq = u; u = vp; vp = vq; vq = u; }
-        mine += jacobi_rotate_pair(wp, wq, vp, vq, n, tol, lane);
+        double *np = NA + j, *nq = NB + k;
+        if (ga > gb) {
+          double* u = wp; wp = wq; wq = u; u = vp; vp = vq; vq = u; u = np; np = nq; nq = u;
+        }
+        mine += jacobi_rotate_tracked(wp, wq, vp, vq, np, nq, n, tol, lane);
       }
       __syncthreads();
     }
@@ -749,9 +683,12 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
       }
       const double* srcW = cluster.map_shared_rank(Wb(sm, x, oslot), owner);
       const double* srcV = cluster.map_shared_rank(Vb(sm, x, oslot), owner);
+      const double* srcN = cluster.map_shared_rank(Nb(sm, x, oslot), owner);
       double* dW = Wb(sm, 1 - x, sl);
       double* dV = Vb(sm, 1 - x, sl);
+      double* dN = Nb(sm, 1 - x, sl);
       for (int64_t t = tid; t < blk; t += nt) { dW[t] = srcW[t]; dV[t] = srcV[t]; }
+      for (int t = tid; t < nb; t += nt) dN[t] = srcN[t];
     }
     __syncthreads();
     x = 1 - x;
@@ -773,6 +710,68 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
     }
   }
   cluster.sync();   // no CTA leaves while another may still read its shared memory
+}
+
+// Grid-wide block Jacobi for larger n (W, V column-major n x n in global memory, L2-resident):
+// one launch per round of the P-block tournament; CTA i rotates the cross pairs of the blocks
+// rr(i, r) and rr(P-1-i, r) (and, in round 0, the pairs inside both), counting its rotations.
+__global__ void __launch_bounds__(256) jacobi_grid_round_kernel(double* W, double* V, int n, int nb,
+                                                                int P, int r, double tol,
+                                                                unsigned* count) {
+  const int i = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int bA = rr_index(i, r, P), bB = rr_index(P - 1 - i, r, P);
+  int mine = 0;
+  auto rotate = [&](int p, int q) {
+    if (p > q) { const int t = p; p = q; q = t; }
+    if (q >= n) return;
+    double* wp = W + (int64_t)p * n;
+    double* wq = W + (int64_t)q * n;
+    double a = 0.0, b = 0.0, g = 0.0;
+    for (int k = lane; k < n; k += 32) {
+      const double x = wp[k], y = wq[k];
+      a = fma(x, x, a); b = fma(y, y, b); g = fma(x, y, g);
+    }
+    a = warp_sum_d(a); b = warp_sum_d(b); g = warp_sum_d(g);
+    double c, sn;
+    if (!jacobi_rotation(a, b, g, tol, c, sn)) return;
+    double* vp = V + (int64_t)p * n;
+    double* vq = V + (int64_t)q * n;
+    for (int k = lane; k < n; k += 32) {
+      const double x = wp[k], y = wq[k];
+      wp[k] = c * x - sn * y;
+      wq[k] = sn * x + c * y;
+      const double u = vp[k], v = vq[k];
+      vp[k] = c * u - sn * v;
+      vq[k] = sn * u + c * v;
+    }
+    ++mine;
+  };
+  if (r == 0) {   // pairs inside each of the two blocks
+    const int m2 = nb + (nb & 1);
+    for (int t = 0; t < m2 - 1; ++t) {
+      for (int task = warp; task < m2; task += nw) {
+        const int sl = task / (m2 / 2), pi = task % (m2 / 2);
+        const int p = rr_index(pi, t, m2), q = rr_index(m2 - 1 - pi, t, m2);
+        if (p >= nb || q >= nb) continue;
+        const int base = (sl ? bB : bA) * nb;
+        rotate(base + p, base + q);
+      }
+      __syncthreads();
+    }
+  }
+  for (int t = 0; t < nb; ++t) {
+    for (int j = warp; j < nb; j += nw) rotate(bA * nb + j, bB * nb + (j + t) % nb);
+    __syncthreads();
+  }
+  if (lane == 0 && mine) atomicAdd(count, (unsigned)mine);
+}
+
+__global__ void identity_kernel(double* V, int n) {
+  const int64_t total = (int64_t)n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x)
+    V[t] = (t % n == t / n) ? 1.0 : 0.0;
 }
 
 // From the rotated W (column-major n x n) and the rotations V: sigma_j = ||W_j||, descending order;
@@ -987,8 +986,10 @@ QRResult qr(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, doubl
   QRResult res;
   res.k = m < n ? m : n;
   if (m <= 0 || n <= 0) return res;
-  // small, wide: single-block Householder (robust, cheap at these sizes)
-  const bool small = (double)m * n * n < 4.0e5;
+  // small or wide: single-block Householder (robust, cheap at these sizes). A tall matrix with
+  // few columns (m >= 1024, e.g. the kickrank-wide z blocks of 5120 rows) is not small: one
+  // block's serial column sweep over m rows costs more than the GEMM passes of CholeskyQR3.
+  const bool small = (double)m * n * n < 4.0e5 && m < 1024;
   if (m < n || small || n > 1024) {
     householder(A, lda, m, n, Q, R, ws, s);
     return res;
@@ -1069,19 +1070,41 @@ void svd(const double* A, int64_t lda, int64_t m, int64_t n, double* U, double* 
   double* Vw = W + n * n;    // 2 n x n: accumulated rotations V' (sorted) and scratch
   transpose(Rb.p, n, W, n, n, n, s);
   DBuf Up((size_t)(n * n), s);   // U' (normalised columns of the rotated R^T, sorted)
-  if (n <= kJacobiClusterMaxN && n >= 2 * kJacobiCluster) {
-    if (n <= kJacobiBlockMaxN) {
-      const int nb = (int)((n + 2 * kJacobiCluster - 1) / (2 * kJacobiCluster));
-      const size_t smem = (size_t)8 * nb * n * sizeof(double);
-      smem_optin((const void*)jacobi_block_kernel, (int)smem);
-      jacobi_block_kernel<<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status);
-    } else {
-      const int ncl = (int)((n + kJacobiCluster - 1) / kJacobiCluster);
-      const size_t smem = (size_t)2 * ncl * n * sizeof(double);
-      smem_optin((const void*)jacobi_cluster_kernel, (int)smem);
-      jacobi_cluster_kernel<<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status);
-    }
+  if (n <= kJacobiBlockMaxN && n >= 2 * kJacobiCluster) {
+    const int nb = (int)((n + 2 * kJacobiCluster - 1) / (2 * kJacobiCluster));
+    const size_t smem = (size_t)4 * (2 * nb * n + nb + (nb & 1)) * sizeof(double);
+    smem_optin((const void*)jacobi_block_kernel, (int)smem);
+    jacobi_block_kernel<<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status);
     TTGB_CHECK_LAUNCH();
+    DBuf sig((size_t)n, s);
+    svd_sort_kernel<<<1, 1024, 0, s>>>(W, Vw, (int)n, Up.p, S, Vw + n * n, sig.p);
+    TTGB_CHECK_LAUNCH();
+    gemm_cm(Qb.p, m, Vw + n * n, n, U, m, m, n, n, 1.0, 0.0, s);   // U = Q V'
+    transpose(Up.p, n, Vh, n, n, n, s);                            // Vh = U'^T
+    return;
+  }
+  if (n > kJacobiBlockMaxN) {   // grid-wide block Jacobi, one launch per round
+    const int sms = num_sms();
+    const int nb = (int)std::max<int64_t>(1, (n + 2 * sms - 1) / (2 * sms));
+    int P = (int)((n + nb - 1) / nb);
+    P += P & 1;
+    identity_kernel<<<cdiv((int64_t)n * n, 256), 256, 0, s>>>(Vw, (int)n);
+    TTGB_CHECK_LAUNCH();
+    DevBuf<unsigned> cnt(1, s);
+    unsigned hcnt = 0;
+    const double tol = std::max((double)n, 1.0) * kEps;
+    int sweep = 0;
+    for (; sweep < 60; ++sweep) {
+      TTGB_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned), s));
+      for (int r = 0; r < P - 1; ++r) {
+        jacobi_grid_round_kernel<<<P / 2, 256, 0, s>>>(W, Vw, (int)n, nb, P, r, tol, cnt.p);
+        TTGB_CHECK_LAUNCH();
+      }
+      TTGB_CUDA(cudaMemcpyAsync(&hcnt, cnt.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+      TTGB_CUDA(cudaStreamSynchronize(s));
+      if (hcnt == 0) break;
+    }
+    if (sweep >= 60) TTGB_CUDA(cudaMemsetAsync(ws.status, 0x03, 1, s));
     DBuf sig((size_t)n, s);
     svd_sort_kernel<<<1, 1024, 0, s>>>(W, Vw, (int)n, Up.p, S, Vw + n * n, sig.p);
     TTGB_CHECK_LAUNCH();
