@@ -167,6 +167,12 @@ int ttgb_tt_matvec(const ttgb_tt* A, const ttgb_tt* x, void* stream, ttgb_soluti
 int ttgb_dmrg_matvec(const ttgb_tt* A, const ttgb_tt* x, const ttgb_tt* y0, int32_t nswp,
                      double eps, int64_t rmax, int32_t kickrank, uint64_t seed, int32_t verbose,
                      void* stream, ttgb_solution** out);
+/* y ~ A b by AMEn (the projection of A b onto the sweep's interfaces with residual enrichment) to
+   relative accuracy eps (replaces torchtt.amen_mv / _amen_mm_python, torchtt/_amen.py:55-101,
+   126-410). x0 may be NULL (zeros of rank 1); the result is a library-owned ttgb_solution. */
+int ttgb_amen_mv(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, int32_t nswp, double eps,
+                 int64_t rmax, int32_t kickrank, int32_t kick2, uint64_t seed, int32_t verbose,
+                 void* stream, ttgb_solution** out);
 /* ||x||_F by a QR sweep (replaces TT.norm, torchtt/_tt_base.py:1021-1051). */
 int ttgb_tt_norm(const ttgb_tt* x, double* out, void* stream);
 /* TT rounding to relative accuracy eps with rank cap rmax; the result is a library-owned

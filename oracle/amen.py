@@ -673,3 +673,165 @@ def dmrg_matvec(A_cores, x_cores, y0_cores=None, nswp=20, eps=1e-12, rmax=32768,
             last = True
         delta_prev = delta.copy()
     return y
+
+
+# --------------------------------------------------------------------------------------------------
+# AMEn matvec (torchtt/_amen.py:126-410, for a TT-vector b)
+# --------------------------------------------------------------------------------------------------
+
+def _local_ab(Pl, Pr, a, b):
+    """Projection of A b: out[l,M,L] = sum Pl[l,s,c] a[s,M,K,S] b[c,K,C] Pr[L,S,C]
+    (_local_AB, torchtt/_amen.py:36-53, for vectors)."""
+    return local_product(Pr, Pl, a, b)
+
+
+def _phi_ab(fwd, Phi, a, b, core):
+    """Interfaces with (A, b) (_compute_phi_bck_AB / _fwd_AB, torchtt/_amen.py:452-487)."""
+    if fwd:
+        return np.einsum('rac,rMR,aMKA,cKC->RAC', Phi, core, a, b, optimize=True)
+    return np.einsum('RAC,rMR,aMKA,cKC->rac', Phi, core, a, b, optimize=True)
+
+
+def _phi_xx(fwd, Phi, left, right):
+    """Interfaces between two cores (_compute_phi_bck_x / _fwd_x, torchtt/_amen.py:416-449)."""
+    if fwd:
+        return np.einsum('lr,lML,rMR->LR', Phi, left, right, optimize=True)
+    return np.einsum('LR,lML,rMR->lr', Phi, left, right, optimize=True)
+
+
+def amen_mv(A_cores, b_cores, x0_cores=None, nswp=22, eps=1e-10, rmax=1024, kickrank=4, kick2=0,
+            rng=None):
+    """y ~ A b by AMEn, restating _amen_mm_python (torchtt/_amen.py:126-410) step by step for a
+    TT-vector b: zeros of rank 1 as the start, random orthogonalised z, right-to-left z update /
+    QR / interface refresh with the normx/normb/nrmsc bookkeeping, left-to-right projection,
+    truncation (rank_chop at eps ||.|| / d^1.5, d^0.5 in the last sweep), z update and enrichment.
+    Random numbers come from `rng` (a numpy Generator)."""
+    rng = rng if rng is not None else np.random.default_rng(0)
+    d = len(A_cores)
+    M = [a.shape[1] for a in A_cores]
+    if x0_cores is None:
+        x = [np.zeros((1, m, 1)) for m in M]
+        rx = [1] * (d + 1)
+    else:
+        x = [c.copy() for c in x0_cores]
+        rx = [1] + [c.shape[2] for c in x]
+    rz = [1] + [kickrank + kick2] * (d - 1) + [1]
+    z = [rng.standard_normal((rz[k], M[k], rz[k + 1])) for k in range(d)]
+    for k in range(d - 1, 0, -1):   # rl_orthogonal
+        q, r = np.linalg.qr(z[k].reshape(rz[k], -1).T)
+        rz[k] = q.shape[1]
+        z[k] = q.T.reshape(rz[k], M[k], rz[k + 1])
+        z[k - 1] = np.tensordot(z[k - 1], r.T, axes=([2], [0]))
+    one2, one3 = np.ones((1, 1)), np.ones((1, 1, 1))
+    Phiz = [one2] + [None] * (d - 1) + [one2]
+    Phiz_rhs = [one3] + [None] * (d - 1) + [one3]
+    Phis = [one2] + [None] * (d - 1) + [one2]
+    Phis_rhs = [one3] + [None] * (d - 1) + [one3]
+    normA, normb, normx = np.ones(d - 1), np.ones(d - 1), np.ones(d - 1)
+    nrmsc = 1.0
+    last = False
+    for swp in range(nswp):
+        for k in range(d - 1, 0, -1):
+            if not last:
+                if swp > 0:
+                    czx = np.einsum('zr,rmR,ZR->zmZ', Phiz[k], x[k], Phiz[k + 1])
+                    czAB = _local_ab(Phiz_rhs[k], Phiz_rhs[k + 1], A_cores[k], b_cores[k])
+                    cz = czAB * nrmsc - czx
+                    _, _, vz = np.linalg.svd(cz.reshape(cz.shape[0], -1), full_matrices=False)
+                    cz = vz[:min(kickrank, vz.shape[0]), :].T
+                    if k < d - 1:
+                        cz = np.concatenate([cz, rng.standard_normal((cz.shape[0], kick2))], 1)
+                else:
+                    cz = z[k].reshape(rz[k], -1).T
+                qz, _ = np.linalg.qr(cz)
+                rz[k] = qz.shape[1]
+                z[k] = qz.T.reshape(rz[k], M[k], rz[k + 1])
+            if swp > 0:
+                nrmsc = nrmsc * normA[k - 1] * normx[k - 1] / normb[k - 1]
+            Q, R = np.linalg.qr(x[k].reshape(rx[k], -1).T)
+            prev = np.tensordot(x[k - 1], R.T, axes=([2], [0]))
+            rx[k] = Q.shape[1]
+            cn = np.linalg.norm(prev)
+            if cn > 0:
+                prev = prev / cn
+            else:
+                cn = 1.0
+            normx[k - 1] *= cn
+            x[k] = Q.T.reshape(rx[k], M[k], rx[k + 1])
+            x[k - 1] = prev
+            Phis[k] = _phi_xx(False, Phis[k + 1], x[k], x[k])
+            Phis_rhs[k] = _phi_ab(False, Phis_rhs[k + 1], A_cores[k], b_cores[k], x[k])
+            nb = np.linalg.norm(Phis_rhs[k])
+            nb = nb if nb > 0 else 1.0
+            normb[k - 1] = nb
+            Phis_rhs[k] = Phis_rhs[k] / nb
+            nrmsc = nrmsc * normb[k - 1] / (normA[k - 1] * normx[k - 1])
+            if not last:
+                Phiz[k] = _phi_xx(False, Phiz[k + 1], z[k], x[k]) / normA[k - 1]
+                Phiz_rhs[k] = _phi_ab(False, Phiz_rhs[k + 1], A_cores[k], b_cores[k], z[k]) / normb[k - 1]
+        max_dx = 0.0
+        for k in range(d):
+            prev = x[k]
+            sol = _local_ab(Phis_rhs[k], Phis_rhs[k + 1], A_cores[k], b_cores[k]) * nrmsc
+            nsol = np.linalg.norm(sol)
+            dx = np.linalg.norm(sol - prev) / nsol
+            max_dx = max(dx, max_dx)
+            sol = sol.reshape(rx[k] * M[k], rx[k + 1])
+            if k < d - 1:
+                u, s, v = np.linalg.svd(sol, full_matrices=False)
+                r = rank_chop(s, nsol * eps / d ** (0.5 if last else 1.5))
+                r = min(r, s.size, rmax)
+            else:
+                u, v = np.linalg.qr(sol)
+                r = u.shape[1]
+                s = np.ones(r)
+            u = u[:, :r]
+            v = (np.diag(s[:r]) @ v[:r, :]).T
+            if not last:
+                czx = np.einsum('zr,rmR,ZR->zmZ', Phiz[k], (u @ v.T).reshape(rx[k], M[k], rx[k + 1]), Phiz[k + 1])
+                czAB = _local_ab(Phiz_rhs[k], Phiz_rhs[k + 1], A_cores[k], b_cores[k])
+                cz = czAB * nrmsc - czx
+                uz, _, _ = np.linalg.svd(cz.reshape(rz[k] * M[k], rz[k + 1]), full_matrices=False)
+                cz = uz[:, :min(kickrank, uz.shape[1])]
+                if k < d - 1:
+                    cz = np.concatenate([cz, rng.standard_normal((cz.shape[0], kick2))], 1)
+                qz, _ = np.linalg.qr(cz)
+                rz[k + 1] = qz.shape[1]
+                z[k] = qz.reshape(rz[k], M[k], rz[k + 1])
+            if k < d - 1:
+                if not last:
+                    czx = np.einsum('zr,rmR,ZR->zmZ', Phis[k], (u @ v.T).reshape(rx[k], M[k], rx[k + 1]), Phiz[k + 1])
+                    czAB = _local_ab(Phis_rhs[k], Phiz_rhs[k + 1], A_cores[k], b_cores[k])
+                    uk = czAB * nrmsc - czx
+                    u, Rm = np.linalg.qr(np.concatenate([u, uk.reshape(u.shape[0], -1)], 1))
+                    v = np.concatenate([v, np.zeros((rx[k + 1], uk.shape[-1]))], 1) @ Rm.T
+                r = u.shape[1]
+                v = np.tensordot(v, x[k + 1], axes=([0], [0]))
+                nrmsc = nrmsc * normA[k] * normx[k] / normb[k]
+                nn = np.linalg.norm(v)
+                if nn > 0:
+                    v = v / nn
+                else:
+                    nn = 1.0
+                normx[k] *= nn
+                x[k] = u.reshape(rx[k], M[k], r)
+                x[k + 1] = v.reshape(r, M[k + 1], rx[k + 2])
+                rx[k + 1] = r
+                Phis[k + 1] = _phi_xx(True, Phis[k], x[k], x[k])
+                Phis_rhs[k + 1] = _phi_ab(True, Phis_rhs[k], A_cores[k], b_cores[k], x[k])
+                nb = np.linalg.norm(Phis_rhs[k + 1])
+                nb = nb if nb > 0 else 1.0
+                normb[k] = nb
+                Phis_rhs[k + 1] = Phis_rhs[k + 1] / nb
+                nrmsc = nrmsc * normb[k] / (normA[k] * normx[k])
+                if not last:
+                    Phiz[k + 1] = _phi_xx(True, Phiz[k], z[k], x[k]) / normA[k]
+                    Phiz_rhs[k + 1] = _phi_ab(True, Phiz_rhs[k], A_cores[k], b_cores[k], z[k]) / normb[k]
+            else:
+                x[k] = (u @ np.diag(s[:r]) @ v[:r, :].T).reshape(rx[k], M[k], rx[k + 1])
+        if last:
+            break
+        if max_dx < eps:
+            last = True
+    f = np.exp(np.sum(np.log(normx)) / d)
+    return [c * f for c in x]

@@ -11,6 +11,7 @@ Python package is imported from the tree. Writes ``tests/golden/*.npz``:
 * ``round.npz`` - inputs and outputs of the reference's TT rounding (``TT.round``);
 * ``divide.npz`` - inputs and outputs of the reference's elementwise division (``amen_divide``);
 * ``dmrg.npz`` - inputs and outputs of the reference's C++ DMRG matvec (``dmrg_mv``);
+* ``amen_mv.npz`` - inputs and outputs of the reference's AMEn matvec and matmat;
 * ``solve_<name>.npz`` - the inputs of a whole solve (A, b, x0 cores, the initial enrichment cores z0
   that the reference drew with ``torch::randn`` after ``torch.manual_seed``), the parameters, and the
   solution cores returned by ``torchttcpp.amen_solve`` (``cpp/amen_solve.h:122``) and, for the small
@@ -158,6 +159,29 @@ def dmrg(cpp):
     print("dmrg.npz written")
 
 
+def amen_products(torchtt):
+    """The reference's AMEn matvec and matmat (torchtt.amen_mv / amen_mm, torchtt/_amen.py:55-125)
+    on a Laplacian-plus-potential operator; their random z cores come from the global torch RNG
+    (seeded here), so parity is on the product."""
+    out = {}
+    A = W.laplace_potential_ttm(5, 8)
+    x = W.random_tt([8] * 5, [1, 3, 3, 3, 3, 1], 31)
+    torch.manual_seed(31)
+    y = torchtt.amen_mv(torchtt.TT(A), torchtt.TT(x), eps=1e-10)
+    _pack_cores("mv_A", A, out)
+    _pack_cores("mv_b", x, out)
+    _pack_cores("mv_y", y.cores, out)
+    B = W.laplace_ttm(4, 6)
+    A2 = W.laplace_potential_ttm(4, 6)
+    torch.manual_seed(32)
+    Y = torchtt.amen_mm(torchtt.TT(A2), torchtt.TT(B), eps=1e-10)
+    _pack_cores("mm_A", A2, out)
+    _pack_cores("mm_B", B, out)
+    _pack_cores("mm_Y", Y.cores, out)
+    np.savez_compressed(os.path.join(HERE, "amen_mv.npz"), **out)
+    print("amen_mv.npz written")
+
+
 def solve_case(torchtt, cpp, wl, seed, prec=None, with_python=False, extra=None):
     A, b, x0 = wl["A"], wl["b"], wl.get("x0")
     p = dict(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
@@ -212,6 +236,7 @@ def main():
     rounding(torchtt)
     division(torchtt)
     dmrg(cpp)
+    amen_products(torchtt)
     small = W.small_random_system(0)
     for prec in (None, "c", "r"):
         solve_case(torchtt, cpp, small, seed=11, prec=prec, with_python=True,

@@ -115,3 +115,13 @@ def test_dmrg_matvec_matches_reference():
         assert [c.shape for c in y] == [c.shape for c in yr], name
         assert O.tt_relerr(y, yr) <= 1e-12
         assert O.tt_relerr(y, O.tt_matvec(A, x)) <= 1e-12
+
+
+def test_amen_mv_matches_reference():
+    """The oracle's AMEn matvec against the reference's torchtt.amen_mv: same ranks, same product."""
+    z = G.load("amen_mv.npz")
+    A, b, yr = G.cores(z, "mv_A"), G.cores(z, "mv_b"), G.cores(z, "mv_y")
+    y = O.amen_mv(A, b, eps=1e-10)
+    assert [c.shape for c in y] == [c.shape for c in yr]
+    assert O.tt_relerr(y, yr) <= 1e-12
+    assert O.tt_relerr(y, O.tt_matvec(A, b)) <= 1e-12

@@ -11,7 +11,8 @@ from . import solvers
 from .solvers import amen_solve
 from .division import amen_divide
 from .dmrg import dmrg_matvec
+from .amen_mv import amen_mm, amen_mv
 
-__all__ = ["TT", "amen_solve", "amen_divide", "dmrg_matvec", "solvers", "errors", "GB300Error", "IncompatibleTypes",
+__all__ = ["TT", "amen_solve", "amen_divide", "dmrg_matvec", "amen_mv", "amen_mm", "solvers", "errors", "GB300Error", "IncompatibleTypes",
            "InvalidArguments", "RankMismatch", "ShapeMismatch"]
 __version__ = "0.1.0"

@@ -89,6 +89,9 @@ _SIGS = {
     "ttgb_dmrg_matvec": (c_i32, [ctypes.POINTER(TTDesc), ctypes.POINTER(TTDesc), ctypes.POINTER(TTDesc),
                                  c_i32, c_dbl, c_i64, c_i32, ctypes.c_uint64, c_i32, c_vp,
                                  ctypes.POINTER(c_vp)]),
+    "ttgb_amen_mv": (c_i32, [ctypes.POINTER(TTDesc), ctypes.POINTER(TTDesc), ctypes.POINTER(TTDesc),
+                             c_i32, c_dbl, c_i64, c_i32, c_i32, ctypes.c_uint64, c_i32, c_vp,
+                             ctypes.POINTER(c_vp)]),
     "ttgb_tt_matvec": (c_i32, [ctypes.POINTER(TTDesc), ctypes.POINTER(TTDesc), c_vp, ctypes.POINTER(c_vp)]),
     "ttgb_tt_norm": (c_i32, [ctypes.POINTER(TTDesc), ctypes.POINTER(c_dbl), c_vp]),
     "ttgb_tt_round": (c_i32, [ctypes.POINTER(TTDesc), c_dbl, c_i64, c_vp, ctypes.POINTER(c_vp)]),

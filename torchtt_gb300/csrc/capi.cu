@@ -16,6 +16,7 @@
 #include "tc_local.cuh"
 #include "tt_ops.cuh"
 #include "dmrg.cuh"
+#include "amen_mv.cuh"
 
 using namespace ttgb;
 
@@ -262,6 +263,27 @@ int ttgb_dmrg_matvec(const ttgb_tt* A, const ttgb_tt* x, const ttgb_tt* y0, int3
     sol->res.cores = dmrg_matvec(va, vx, vy, p, sc.s, sol->res.ranks, &st, sc.lws, sc.red);
     sol->res.stats.sweeps = st.sweeps;
     sol->res.stats.max_res = st.max_delta;
+    *out = sol.release();
+  });
+}
+
+int ttgb_amen_mv(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, int32_t nswp, double eps,
+                 int64_t rmax, int32_t kickrank, int32_t kick2, uint64_t seed, int32_t verbose,
+                 void* stream, ttgb_solution** out) {
+  return guarded([&] {
+    TTGB_REQUIRE(A && b && out && A->d > 0 && A->d == b->d, "bad AMEn matvec arguments");
+    TTGB_REQUIRE(A->rows != nullptr && b->rows == nullptr,
+                 "A must be TT-matrix and b must be vector.");
+    const TTView va = view_of(A, true), vb = view_of(b, false), vx = view_of(x0, false);
+    AmenMvParams p;
+    p.nswp = nswp; p.eps = eps; p.rmax = rmax; p.kickrank = kickrank; p.kick2 = kick2;
+    p.seed = seed; p.verbose = verbose;
+    Scratch sc(as_stream(stream));
+    std::unique_ptr<ttgb_solution> sol(new ttgb_solution());
+    AmenMvStats st;
+    sol->res.cores = amen_mv(va, vb, vx, p, sc.s, sol->res.ranks, &st, sc.lws, sc.red);
+    sol->res.stats.sweeps = st.sweeps;
+    sol->res.stats.max_res = st.max_dx;
     *out = sol.release();
   });
 }
