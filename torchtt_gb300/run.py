@@ -1,9 +1,13 @@
 """Command-line solve of a named synthetic workload (also the target of profiler runs).
 
   python -m torchtt_gb300.run --workload laplace_d8_n16 --solves 1 [--seed 1] [--verbose]
+  python -m torchtt_gb300.run --workload parametric_diffusion_d10_n32 --solves 32 --served 8
 
-Runs the solves one after another on cuda:0 and prints one line of statistics per solve. It starts
-no helper processes, so a profiler attached to it sees only this process's kernels.
+Runs the solves one after another on cuda:0 and prints one line of statistics per solve; with
+``--served K`` it submits all of them at once to a request server with K slots (for the
+parametric workload, system i of the batch is the i-th index) and prints one line with the
+throughput, the p50/p99 latency and the worst relative residual. It starts no helper processes,
+so a profiler attached to it sees only this process's kernels.
 """
 import argparse
 import json
@@ -30,7 +34,11 @@ def main():
                     help="low-precision engine of the mixed path")
     ap.add_argument("--no-check", action="store_true",
                     help="skip the relative residual (runs no kernel after the solve)")
+    ap.add_argument("--served", type=int, default=0,
+                    help="submit all solves at once to a server with this many slots")
     args = ap.parse_args()
+    if args.served > 0:
+        return served(args)
     if args.workload == "laplace_d8_n16":
         wl = W.laplace_d8_n16(args.seed)
     elif args.workload == "laplace_potential_d20_n64":
@@ -57,6 +65,45 @@ def main():
                           "ranks": st["ranks"], "matvecs": st["matvecs"],
                           "lowp_matvecs": st["lowp_matvecs"], "refinements": st["refinements"],
                           "gmres_iterations": st["gmres_iterations"]}), flush=True)
+
+
+def served(args):
+    import torch
+
+    from . import workloads as W
+    from .serving import Server
+    from .tt import TT
+
+    dev = torch.device("cuda", 0)
+    systems = []
+    for i in range(args.solves):
+        if args.workload == "parametric_diffusion_d10_n32":
+            wl = W.parametric_diffusion_d10_n32(args.index + i, args.seed)
+        elif args.workload == "laplace_d8_n16":
+            wl = W.laplace_d8_n16(args.seed + i)
+        else:
+            wl = W.laplace_potential_d20_n64(args.seed + i)
+        systems.append((TT([c.to(dev) for c in wl["A"]]), TT([c.to(dev) for c in wl["b"]]),
+                        wl["params"]))
+    torch.cuda.synchronize()
+    with Server(slots=args.served, device=dev) as srv:
+        t0 = time.perf_counter()
+        ids = [srv.submit(A, b, precision=args.precision, engine=args.engine, seed=args.seed + i,
+                          eps=p["eps"], nswp=p.get("nswp", 22), kickrank=p["kickrank"])
+               for i, (A, b, p) in enumerate(systems)]
+        res = [srv.result(r) for r in ids]
+        elapsed = time.perf_counter() - t0
+    lat = sorted(st["queue_ms"] + st["run_ms"] for _, st in res)
+    pick = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
+    worst = None
+    if not args.no_check:
+        worst = max(float((A @ x - b).norm() / b.norm()) / p["eps"]
+                    for (A, b, p), (x, _) in zip(systems, res))
+    print(json.dumps({"workload": args.workload, "solves": args.solves, "slots": args.served,
+                      "precision": args.precision, "solves_per_s": args.solves / elapsed,
+                      "elapsed_s": elapsed, "latency_ms": {"p50": pick(0.5), "p99": pick(0.99)},
+                      "max_rank": max(max(st["ranks"]) for _, st in res),
+                      "max_relres_over_eps": worst}), flush=True)
 
 
 if __name__ == "__main__":
