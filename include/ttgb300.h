@@ -193,11 +193,14 @@ int ttgb_local_product(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, i
 
 /* The local product with a low-precision engine (the operator of the mixed path's inner GMRES):
  * FP64 in and out, contraction in TTGB_ENGINE_FP32 (CUDA-core FFMA) or TTGB_ENGINE_TC
- * (tcgen05 tensor cores, 3xTF32 with FP32 accumulation in tensor memory). Same shapes as
+ * (tcgen05 tensor cores, 3xTF32 with FP32 accumulation in tensor memory); TTGB_ENGINE_DF is the
+ * mixed path's FP64-class engine for its residual products (double-float arithmetic on the FP32
+ * pipe, ~1e-13 relative for operands within the FP32 exponent range). Same shapes as
  * ttgb_local_product with one right-hand side. No counterpart in the reference (its only mixed mode
  * is the FP32 GMRES of torchtt/solvers.py:469-496). */
 #define TTGB_ENGINE_FP32 1
 #define TTGB_ENGINE_TC 2
+#define TTGB_ENGINE_DF 3
 int ttgb_local_product_lowp(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, int64_t S,
                             int64_t RL, int64_t R, const double* phi_l, const double* A,
                             const double* phi_r, const double* x, double* y, int32_t engine,
@@ -258,6 +261,15 @@ int64_t ttgb_launch_count(void);
 /* Measured peak of this GPU's FMA pipe in TFLOP/s (dtype 0: FP64, 1: FP32): independent FMA
    chains on every SM, best of three timed launches (about 50 ms each). */
 int ttgb_calibrate_fma(int32_t dtype, double* tflops);
+
+/* Tile autotuner of the contraction engine (no counterpart in the reference): the first launch of
+   each shape class (engine, power-of-two buckets of M, N, K and batch, triangular flags, unit
+   strides, device) that overwrites its output times every tile shape with and without split-K on
+   the caller's stream and keeps the fastest for the process. mode 1 turns it on (the default
+   unless the environment sets TTGB_AUTOTUNE=0), 0 off (occupancy heuristic), any other value only
+   queries; returns the previous state. ttgb_autotune_classes gives the number of recorded classes. */
+int ttgb_autotune(int32_t mode);
+int64_t ttgb_autotune_classes(void);
 
 /* Message of the last error on this thread. */
 const char* ttgb_last_error(void);

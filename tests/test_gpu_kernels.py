@@ -183,3 +183,28 @@ def test_structured_a_stage(cuda, k, rR):
     Pb = g.standard_normal((R + 2, S, R))
     close(ops.compute_phi_bck_A(t(Pb, cuda), t(z, cuda), t(A, cuda), t(x, cuda)),
           O.compute_phi_bck_A(Pb, z, A, x))
+
+
+def test_autotuner_records_classes_and_keeps_results(cuda):
+    """The tile autotuner (times every tile shape with and without split-K on the first launch of
+    a shape class, then reuses the record) gives the oracle's local product, the same as the
+    occupancy heuristic, and records the classes it tuned."""
+    from torchtt_gb300 import ops
+    g = np.random.default_rng(77)
+    r, s, n, S, R = 45, 3, 40, 3, 37
+    PhiL, A = g.standard_normal((r, s, r)), g.standard_normal((s, n, n, S))
+    PhiR, x = g.standard_normal((R, S, R)), g.standard_normal((r, n, R))
+    ref = O.local_product(PhiR, PhiL, A, x)
+    prev, _ = ops.autotune(False)
+    try:
+        y_off = ops.local_product(t(PhiR, cuda), t(PhiL, cuda), t(A, cuda), t(x, cuda))
+        ops.autotune(True)
+        _, before = ops.autotune(None)
+        y_tune = ops.local_product(t(PhiR, cuda), t(PhiL, cuda), t(A, cuda), t(x, cuda))
+        _, after = ops.autotune(None)
+        y_rec = ops.local_product(t(PhiR, cuda), t(PhiL, cuda), t(A, cuda), t(x, cuda))
+    finally:
+        ops.autotune(prev)
+    assert after >= before
+    for y in (y_off, y_tune, y_rec):
+        close(y, ref)

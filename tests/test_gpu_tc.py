@@ -27,3 +27,27 @@ def test_lowp_local_product(cuda, engine, shape):
     err = np.linalg.norm(y - ref) / np.linalg.norm(ref)
     assert err < 1e-5, err
     assert np.abs(y - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("shape", [(60, 3, 64, 3, 60), (1, 3, 64, 3, 9), (171, 2, 32, 2, 20),
+                                   (5, 2, 12, 2, 7)])
+def test_double_float_local_product(cuda, shape):
+    """The mixed path's FP64-class engine (double-float arithmetic on the FP32 pipe, operands split
+    from their bits) against the FP64 oracle, on operands with mixed signs, exact zeros and values
+    spread over 2^-20..2^20 (products stay inside the FP32 range): every entry within 1e-12 of
+    the sum of the absolute values of its terms (the oracle's product of the absolute operands)."""
+    from torchtt_gb300 import ops
+    r, s, n, S, R = shape
+    g = np.random.default_rng(sum(shape) + 31)
+
+    def spread(*dims):
+        v = g.standard_normal(dims) * np.exp2(g.integers(-20, 21, size=dims))
+        v[g.random(dims) < 0.1] = 0.0
+        return v
+
+    PhiL, A, PhiR, x = spread(r, s, r), spread(s, n, n, S), spread(R, S, R), spread(r, n, R)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    y = ops.local_product_lowp(t(PhiR), t(PhiL), t(A), t(x), engine=ops.ENGINE_DF).cpu().numpy()
+    ref = O.local_product(PhiR, PhiL, A, x)
+    bound = O.local_product(np.abs(PhiR), np.abs(PhiL), np.abs(A), np.abs(x))
+    assert np.all(np.abs(y - ref) <= 1e-12 * bound + 1e-300)

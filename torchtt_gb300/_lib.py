@@ -96,6 +96,8 @@ _SIGS = {
     "ttgb_tt_norm": (c_i32, [ctypes.POINTER(TTDesc), ctypes.POINTER(c_dbl), c_vp]),
     "ttgb_tt_round": (c_i32, [ctypes.POINTER(TTDesc), c_dbl, c_i64, c_vp, ctypes.POINTER(c_vp)]),
     "ttgb_launch_count": (c_i64, []),
+    "ttgb_autotune": (c_i32, [c_i32]),
+    "ttgb_autotune_classes": (c_i64, []),
     "ttgb_calibrate_fma": (c_i32, [c_i32, ctypes.POINTER(c_dbl)]),
     "ttgb_last_error": (ctypes.c_char_p, []),
     "ttgb_version": (c_i32, []),

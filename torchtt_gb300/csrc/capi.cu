@@ -337,10 +337,17 @@ int ttgb_local_product_lowp(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t
     TTGB_REQUIRE(rl > 0 && s > 0 && r > 0 && m > 0 && n > 0 && S > 0 && RL > 0 && R > 0,
                  "non-positive dimension");
     TTGB_REQUIRE(phi_l && A && phi_r && x && y, "null pointer");
-    TTGB_REQUIRE(engine == TTGB_ENGINE_FP32 || engine == TTGB_ENGINE_TC, "unknown engine");
+    TTGB_REQUIRE(engine == TTGB_ENGINE_FP32 || engine == TTGB_ENGINE_TC ||
+                     engine == TTGB_ENGINE_DF, "unknown engine");
     cudaStream_t st = as_stream(stream);
     LocalOpDims d{rl, s, r, m, n, S, RL, R};
-    if (engine == TTGB_ENGINE_TC) {
+    if (engine == TTGB_ENGINE_DF) {
+      Fp64EngineScope eng(kFp64DoubleFloat);
+      DBuf w1(local_product_w1(d), st), w2(local_product_w2(d), st);
+      SparseCore sp;
+      sp.build(A, s, m, n, S, st);
+      local_product(d, phi_l, A, phi_r, x, y, w1.p, w2.p, st, 1.0, 0.0, &sp);
+    } else if (engine == TTGB_ENGINE_TC) {
       TTGB_REQUIRE(tc_available(), "tcgen05 engine needs an sm_100-family GPU");
       int* err = nullptr;
       TTGB_CUDA(cudaMallocAsync((void**)&err, sizeof(int), st));
@@ -499,6 +506,10 @@ int ttgb_local_gmres(int64_t r, int64_t s, int64_t n, int64_t S, int64_t R, cons
 const char* ttgb_last_error(void) { return g_last_error.c_str(); }
 
 int64_t ttgb_launch_count(void) { return launch_count(); }
+
+int ttgb_autotune(int32_t mode) { return set_autotune(mode); }
+
+int64_t ttgb_autotune_classes(void) { return autotune_classes(); }
 
 int ttgb_calibrate_fma(int32_t dtype, double* tflops) {
   return guarded([&] {

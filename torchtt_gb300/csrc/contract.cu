@@ -8,7 +8,11 @@
 // tile leaves SMs idle.
 #include <climits>
 
+#include <atomic>
+#include <cstdlib>
+#include <mutex>
 #include <type_traits>
+#include <unordered_map>
 
 #include "contract.cuh"
 
@@ -149,9 +153,30 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams<T> p) {
 // with an error-free two-sum per step. About 10 FP32 operations per multiply-add: on GB300, where
 // the FP32 pipe is ~60x the FP64 pipe, this is several times the FP64 rate at ~1e-13 relative
 // accuracy (operands within the FP32 exponent range).
+//
+// The split is built from the bits of x with integer operations: h keeps the sign, the exponent
+// and the top 23 stored mantissa bits (truncation), l is the remaining 29 mantissa bits converted
+// to FP32 (round to nearest) and scaled by the exponent, so x = h + l to 2^-47 relative. The obvious
+// form h = (float)x, l = (float)(x - h) runs two conversions and a subtraction on the FP64 pipe for
+// every loaded element; on GB300 that pipe then bounds the kernel (ncu: FP64 pipe 51% active
+// against 31% for the FP32 FMA pipe).
 __device__ __forceinline__ void df_split(double x, float& h, float& l) {
-  h = (float)x;
-  l = (float)(x - (double)h);
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+  const unsigned sign = hi & 0x80000000u;
+  const int fe = (int)((hi >> 20) & 0x7ffu) - 896;   // biased FP32 exponent of x (1023 - 127)
+  if (fe >= 1 && fe <= 254) {
+    h = __uint_as_float(sign | ((unsigned)fe << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+    const float r =
+        __uint2float_rn(lo & 0x1fffffffu) * 0x1p-52f * __uint_as_float((unsigned)fe << 23);
+    l = __uint_as_float(__float_as_uint(r) | sign);
+  } else if (((hi & 0x7fffffffu) | lo) == 0u) {   // +-0 (also every masked load)
+    h = __uint_as_float(sign);
+    l = 0.f;
+  } else {   // outside the FP32 range: the engine is only chosen when operands fit
+    h = (float)x;
+    l = 0.f;
+  }
 }
 
 template <int BM, int BN>
@@ -291,38 +316,70 @@ AxD to_dev(const Ax& a, int extent) {
 
 thread_local int t_fp64_engine = kFp64Native;
 
+// ---------------------------------------------------------------------------------------------
+// Tile autotuner. A launch is described by its shape class: the engine (FP64, double-float,
+// FP32), power-of-two buckets of M, N, K and the batch, the triangular flags and which operand
+// strides are unit, and the device. The first launch of a class with beta == 0 (the output is
+// overwritten, so running it several times is harmless) and no overlap between C and its inputs
+// times every candidate - the four tile shapes, each with and without split-K - with CUDA events
+// on the caller's stream (best of two runs) and records the fastest; later launches of the class
+// use the record. Launches that cannot be tuned (beta != 0, aliasing, a capturing stream, a
+// deterministic request) and classes being tuned by another thread use the occupancy heuristic.
+// ---------------------------------------------------------------------------------------------
+struct TileCfg {
+  int bm, bn, split;   // split: 0 no split-K, 1 split-K sized to fill the GPU
+};
+constexpr TileCfg kCandidates[] = {{64, 64, 0}, {64, 32, 0}, {32, 64, 0}, {32, 32, 0},
+                                   {64, 64, 1}, {64, 32, 1}, {32, 64, 1}, {32, 32, 1}};
+constexpr int kNumCandidates = (int)(sizeof(kCandidates) / sizeof(kCandidates[0]));
+
+std::atomic<int> g_autotune{-1};   // -1: not read yet from TTGB_AUTOTUNE
+std::mutex g_tune_mu;
+std::unordered_map<uint64_t, int> g_tune_table;   // class -> candidate index (-1: being tuned)
+std::atomic<int64_t> g_tune_runs{0};
+
+bool autotune_on() {
+  int v = g_autotune.load();
+  if (v < 0) {
+    const char* e = std::getenv("TTGB_AUTOTUNE");
+    v = (e && e[0] == '0') ? 0 : 1;
+    g_autotune.store(v);
+  }
+  return v == 1;
+}
+
+int log2_bucket(int64_t v) {
+  int b = 0;
+  while ((int64_t(1) << b) < v && b < 40) ++b;
+  return b;
+}
+
+// largest address offset of an index of the given extent
+int64_t ax_span(const Ax& a, int64_t extent) {
+  if (extent <= 0) return 0;
+  if (a.e0 >= extent) return (extent - 1) * a.s0;
+  return (a.e0 - 1) * a.s0 + ((extent - 1) / a.e0) * a.s1;
+}
+
 template <typename T>
-void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool deterministic) {
-  if (d.M <= 0 || d.N <= 0 || d.batch <= 0) return;
-  KParams<T> p;
-  p.M = d.M; p.N = d.N; p.K = d.K; p.batch = d.batch;
-  p.A = d.A; p.am = to_dev(d.am, d.M); p.ak = to_dev(d.ak, d.K); p.a_bs = d.a_bs;
-  p.B = d.B; p.bk = to_dev(d.bk, d.K); p.bn = to_dev(d.bn, d.N); p.b_bs = d.b_bs;
-  p.C = d.C; p.cm = to_dev(d.cm, d.M); p.cn = to_dev(d.cn, d.N); p.c_bs = d.c_bs;
-  p.alpha = d.alpha; p.beta = d.beta;
-  p.tri = d.tri;
-  if (d.K <= 0) {  // empty sum: C = beta * C
-    scale_output_kernel<<<cdiv((int64_t)d.M * d.N * d.batch, 256) > 4096 ? 4096 : cdiv((int64_t)d.M * d.N * d.batch, 256), 256, 0, stream>>>(
-        p.C, p.M, p.N, p.batch, p.cm, p.cn, p.c_bs, p.beta);
-    TTGB_CHECK_LAUNCH();
-    return;
-  }
-  const int sms = num_sms();
-  auto tiles = [&](int bm, int bn) { return (int64_t)cdiv(d.M, bm) * cdiv(d.N, bn) * d.batch; };
-  int bm = 64, bn = 64;
+bool overlaps(const T* x, int64_t xs, const T* y, int64_t ys) {
+  return x < y + ys + 1 && y < x + xs + 1;
+}
+
+template <typename T>
+int heuristic_split(const ContractDescT<T>& d, int bm, int bn, int sms, bool force) {
+  const int64_t t = (int64_t)cdiv(d.M, bm) * cdiv(d.N, bn) * d.batch;
   const int64_t target = 2 * (int64_t)sms;
-  if (tiles(64, 64) < target) {
-    if (d.M >= d.N) { bm = 64; bn = 32; } else { bm = 32; bn = 64; }
-    if (tiles(bm, bn) < target) { bm = 32; bn = 32; }
-  }
-  int splitk = 1;
-  const int64_t t = tiles(bm, bn);
-  if (!deterministic && t < sms && d.K >= 128) {
-    splitk = (int)((target + t - 1) / t);
-    int maxsplit = d.K / 64;
-    if (splitk > maxsplit) splitk = maxsplit;
-    if (splitk < 1) splitk = 1;
-  }
+  if (!force && !(t < sms && d.K >= 128)) return 1;
+  int splitk = (int)((target + t - 1) / t);
+  const int maxsplit = d.K / 64;
+  if (splitk > maxsplit) splitk = maxsplit;
+  return splitk < 1 ? 1 : splitk;
+}
+
+template <typename T>
+void launch_tiles(const ContractDescT<T>& d, KParams<T> p, int bm, int bn, int splitk,
+                  cudaStream_t stream) {
   int kchunk = d.K;
   if (splitk > 1) {
     kchunk = (int)cdiv(cdiv(d.K, splitk), BK) * BK;
@@ -356,7 +413,128 @@ void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool determ
   TTGB_CHECK_LAUNCH();
 }
 
+template <typename T>
+uint64_t tune_key(const ContractDescT<T>& d) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int eng = std::is_same<T, float>::value ? 2 : (t_fp64_engine == kFp64DoubleFloat ? 1 : 0);
+  const int units = (d.am.s0 == 1) | ((d.ak.s0 == 1) << 1) | ((d.bk.s0 == 1) << 2) |
+                    ((d.bn.s0 == 1) << 3) | ((d.cm.s0 == 1) << 4);
+  uint64_t k = (uint64_t)eng;
+  k = k * 64 + (uint64_t)log2_bucket(d.M);
+  k = k * 64 + (uint64_t)log2_bucket(d.N);
+  k = k * 64 + (uint64_t)log2_bucket(d.K);
+  k = k * 64 + (uint64_t)log2_bucket(d.batch);
+  k = k * 4 + (uint64_t)(d.tri & 3);
+  k = k * 32 + (uint64_t)units;
+  k = k * 64 + (uint64_t)(dev & 63);
+  return k;
+}
+
+// Returns the candidate index to use, tuning the class first when this launch may be repeated.
+// -1: use the heuristic. A tuned launch has already written C (tuned = true).
+template <typename T>
+int tuned_choice(const ContractDescT<T>& d, const KParams<T>& p, cudaStream_t stream,
+                 bool& tuned) {
+  tuned = false;
+  if (d.beta != T(0)) return -1;
+  const int64_t sa = (d.batch - 1) * d.a_bs + ax_span(d.am, d.M) + ax_span(d.ak, d.K);
+  const int64_t sb = (d.batch - 1) * d.b_bs + ax_span(d.bk, d.K) + ax_span(d.bn, d.N);
+  const int64_t sc = (d.batch - 1) * d.c_bs + ax_span(d.cm, d.M) + ax_span(d.cn, d.N);
+  if (overlaps<T>(d.C, sc, d.A, sa) || overlaps<T>(d.C, sc, d.B, sb)) return -1;
+  const uint64_t key = tune_key(d);
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune_table.find(key);
+    if (it != g_tune_table.end()) return it->second;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+      return -1;
+    g_tune_table[key] = -1;   // being tuned: other threads use the heuristic meanwhile
+  }
+  const int sms = num_sms();
+  cudaEvent_t ev[2];
+  TTGB_CUDA(cudaEventCreate(&ev[0]));
+  TTGB_CUDA(cudaEventCreate(&ev[1]));
+  int best = -1;
+  float best_ms = 0.f;
+  for (int rep = 0; rep < 2; ++rep) {
+    for (int c = 0; c < kNumCandidates; ++c) {
+      const TileCfg& t = kCandidates[c];
+      const int split = t.split ? heuristic_split(d, t.bm, t.bn, sms, true) : 1;
+      if (t.split && split == 1) continue;   // the same launch as the unsplit candidate
+      TTGB_CUDA(cudaEventRecord(ev[0], stream));
+      launch_tiles(d, p, t.bm, t.bn, split, stream);
+      TTGB_CUDA(cudaEventRecord(ev[1], stream));
+      TTGB_CUDA(cudaEventSynchronize(ev[1]));
+      float ms = 0.f;
+      TTGB_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+      if (rep == 1 && (best < 0 || ms < best_ms)) { best = c; best_ms = ms; }
+    }
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  g_tune_runs.fetch_add(1);
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tune_table[key] = best;
+  }
+  tuned = true;   // every candidate overwrote C with the full result
+  return best;
+}
+
+template <typename T>
+void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool deterministic) {
+  if (d.M <= 0 || d.N <= 0 || d.batch <= 0) return;
+  KParams<T> p;
+  p.M = d.M; p.N = d.N; p.K = d.K; p.batch = d.batch;
+  p.A = d.A; p.am = to_dev(d.am, d.M); p.ak = to_dev(d.ak, d.K); p.a_bs = d.a_bs;
+  p.B = d.B; p.bk = to_dev(d.bk, d.K); p.bn = to_dev(d.bn, d.N); p.b_bs = d.b_bs;
+  p.C = d.C; p.cm = to_dev(d.cm, d.M); p.cn = to_dev(d.cn, d.N); p.c_bs = d.c_bs;
+  p.alpha = d.alpha; p.beta = d.beta;
+  p.tri = d.tri;
+  if (d.K <= 0) {  // empty sum: C = beta * C
+    scale_output_kernel<<<cdiv((int64_t)d.M * d.N * d.batch, 256) > 4096 ? 4096 : cdiv((int64_t)d.M * d.N * d.batch, 256), 256, 0, stream>>>(
+        p.C, p.M, p.N, p.batch, p.cm, p.cn, p.c_bs, p.beta);
+    TTGB_CHECK_LAUNCH();
+    return;
+  }
+  const int sms = num_sms();
+  if (!deterministic && autotune_on()) {
+    bool tuned = false;
+    const int c = tuned_choice(d, p, stream, tuned);
+    if (tuned) return;
+    if (c >= 0) {
+      const TileCfg& t = kCandidates[c];
+      launch_tiles(d, p, t.bm, t.bn, t.split ? heuristic_split(d, t.bm, t.bn, sms, true) : 1,
+                   stream);
+      return;
+    }
+  }
+  // occupancy heuristic: the largest tile whose grid still gives two CTAs per SM, split-K when
+  // even 32 x 32 tiles leave SMs idle
+  auto tiles = [&](int bm, int bn) { return (int64_t)cdiv(d.M, bm) * cdiv(d.N, bn) * d.batch; };
+  int bm = 64, bn = 64;
+  const int64_t target = 2 * (int64_t)sms;
+  if (tiles(64, 64) < target) {
+    if (d.M >= d.N) { bm = 64; bn = 32; } else { bm = 32; bn = 64; }
+    if (tiles(bm, bn) < target) { bm = 32; bn = 32; }
+  }
+  launch_tiles(d, p, bm, bn, deterministic ? 1 : heuristic_split(d, bm, bn, sms, false), stream);
+}
+
 }  // namespace
+
+int set_autotune(int mode) {
+  const int prev = autotune_on() ? 1 : 0;
+  if (mode == 0 || mode == 1) g_autotune.store(mode);
+  return prev;
+}
+
+int64_t autotune_classes() {
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  return (int64_t)g_tune_table.size();
+}
 
 Fp64EngineScope::Fp64EngineScope(int engine) : prev_(t_fp64_engine) { t_fp64_engine = engine; }
 Fp64EngineScope::~Fp64EngineScope() { t_fp64_engine = prev_; }

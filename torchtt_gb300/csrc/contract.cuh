@@ -56,11 +56,17 @@ struct Fp64EngineScope {
   int prev_;
 };
 
-// Launches the contraction on `stream`. Picks a split-K factor when the output has too few tiles
-// to fill the GPU (then C is pre-scaled by beta and partial sums are added atomically).
+// Launches the contraction on `stream`. The tile shape and split-K (C pre-scaled by beta, partial
+// sums added atomically) come from the tile autotuner's record for the launch's shape class, or
+// from an occupancy heuristic (deterministic requests never split K).
 void contract(const ContractDesc& d, cudaStream_t stream, bool deterministic = false);
 // The same engine in FP32 (CUDA-core FFMA), for the low-precision local operator.
 void contract(const ContractDescF& d, cudaStream_t stream, bool deterministic = false);
+// Tile autotuner switch: 1 on (default unless TTGB_AUTOTUNE=0), 0 off, other values only query.
+// Returns the previous state.
+int set_autotune(int mode);
+// Number of shape classes with a record (including classes being tuned).
+int64_t autotune_classes();
 
 // Local AMEn product y[l,m,L] = sum Phi_left[l,s,r] A[s,m,n,S] Phi_right[L,S,R] x[r,n,R]
 // (reference: local_product, cpp/amen_solve.h:17-27). `w1` needs r_l*s*n*R and `w2` r_l*m*S*R

@@ -232,8 +232,8 @@ __global__ void trinv_kernel(const double* __restrict__ R, double* Ri, int n) {
 // Single-block Householder QR (LAPACK dgeqrf/dorgqr scheme): W (m x n col-major, ld m) is
 // overwritten; outputs Q (m x k, ld m) and R (k x n, ld k), k = min(m, n).
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) householder_kernel(double* W, int m, int n, double* Q,
-                                                          double* R, double* tau) {
+__device__ __forceinline__ void householder_body(double* W, int m, int n, double* Q, double* R,
+                                                 double* tau) {
   __shared__ double sh[32];
   __shared__ double refl[3];
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -301,6 +301,35 @@ __global__ void __launch_bounds__(512) householder_kernel(double* W, int m, int 
     }
     __syncthreads();
   }
+}
+
+__global__ void __launch_bounds__(512) householder_kernel(double* W, int m, int n, double* Q,
+                                                          double* R, double* tau) {
+  householder_body(W, m, n, Q, R, tau);
+}
+
+// The same factorisation with W, Q and tau in shared memory (m * n + m * k + k doubles), read
+// straight from A (ld lda): every step of the column sweep is a shared-memory access instead of an
+// L2 round trip, which is what bounds the small QRs of the enrichment blocks (m <= 1024, n <= 16).
+constexpr int kHouseholderSmemBytes = 200 * 1024;
+
+__global__ void __launch_bounds__(512, 1) householder_smem_kernel(const double* __restrict__ A,
+                                                               int64_t lda, int m, int n,
+                                                               double* Qout, double* R) {
+  extern __shared__ double hs[];
+  const int k = min(m, n);
+  double* W = hs;
+  double* Q = W + (int64_t)m * n;
+  double* tau = Q + (int64_t)m * k;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int64_t t = tid; t < (int64_t)m * n; t += nt) {
+    const int64_t i = t % m, j = t / m;
+    W[t] = A[j * lda + i];
+  }
+  __syncthreads();
+  householder_body(W, m, n, Q, R, tau);
+  __syncthreads();
+  for (int64_t t = tid; t < (int64_t)m * k; t += nt) Qout[t] = Q[t];
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -916,6 +945,13 @@ void read_status(LinalgWS& ws, cudaStream_t s, int* out) {
 void householder(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, double* R,
                  LinalgWS& ws, cudaStream_t s) {
   const int64_t k = m < n ? m : n;
+  const size_t smem = (size_t)(m * n + m * k + k) * sizeof(double);
+  if (smem <= (size_t)kHouseholderSmemBytes) {
+    smem_optin((const void*)householder_smem_kernel, kHouseholderSmemBytes);
+    householder_smem_kernel<<<1, 512, smem, s>>>(A, lda, (int)m, (int)n, Q, R);
+    TTGB_CHECK_LAUNCH();
+    return;
+  }
   ws.d.ensure(m * n + k + 16, s);
   double* W = ws.d.p;
   double* tau = W + m * n;

@@ -129,11 +129,13 @@ def local_gmres(Phi_left, coreA, Phi_right, rhs, iters=40, threshold=1e-10, rese
 
 ENGINE_FP32 = 1
 ENGINE_TC = 2
+ENGINE_DF = 3
 
 
 def local_product_lowp(Phi_right, Phi_left, coreA, core, engine=ENGINE_TC):
     """The local product with a low-precision engine (FP32 CUDA cores or tcgen05 3xTF32),
-    FP64 in and out: the operator of the mixed path's inner GMRES."""
+    FP64 in and out: the operator of the mixed path's inner GMRES. ``ENGINE_DF`` runs the mixed
+    path's FP64-class products instead (double-float arithmetic on the FP32 pipe)."""
     _dev64(Phi_right, Phi_left, coreA, core)
     rl, s, r = Phi_left.shape
     _, m, n, S = coreA.shape
@@ -151,3 +153,11 @@ def calibrate_fma(dtype="fp64"):
     out = ctypes.c_double()
     _lib.check(_lib.lib().ttgb_calibrate_fma({"fp64": 0, "fp32": 1}[dtype], ctypes.byref(out)))
     return out.value
+
+
+def autotune(mode=None):
+    """Tile autotuner of the contraction engine: ``True`` on, ``False`` off (occupancy heuristic),
+    ``None`` only queries. Returns the previous state and the number of recorded shape classes."""
+    L = _lib.lib()
+    prev = L.ttgb_autotune(-1 if mode is None else int(bool(mode)))
+    return bool(prev), int(L.ttgb_autotune_classes())

@@ -66,6 +66,7 @@ def replay(count, rate, slots=8, precision="mixed", engine="auto", seed=5, mem_b
             rr = float((A @ x - b).norm() / b.norm())
             worst = max(worst, rr / w["params"]["eps"])
         out["max_relres_over_eps"] = worst
+        out["unconverged"] = sum(1 for _, st in results if not st.get("converged", 1))
     return out
 
 
