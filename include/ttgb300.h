@@ -70,8 +70,9 @@ typedef struct ttgb_amen_params {
                                    operators) are applied from their nonzeros; 0: always dense */
   int32_t fp64_engine;          /* FP64 products of local matvecs, interfaces and local rhs:
                                    0 auto (double-float arithmetic on the FP32 pipe on the MIXED
-                                   path when A and b fit the FP32 exponent range, ~1e-13
-                                   relative; native FP64 otherwise), 1 native FP64, 2 double-float.
+                                   path when eps >= 1e-9 and A and b fit the FP32 exponent range,
+                                   ~1e-13 relative; native FP64 otherwise), 1 native FP64,
+                                   2 double-float.
                                    QR and SVD always run in native FP64. */
 } ttgb_amen_params;
 

@@ -117,6 +117,26 @@ def test_svd(cuda, mn):
     assert np.abs(vh @ vh.T - np.eye(k)).max() < 1e-12
 
 
+def test_svd_clustered_and_rank_deficient(cuda):
+    """Repeated singular values, a spectrum down to 1e-14 and exact zeros in the cluster Jacobi
+    range (16 <= n <= 160), where FP32 sweeps precondition the FP64 ones: the FP32 phase cannot
+    resolve the clustered or tiny values and the FP64 sweeps must finish them."""
+    from torchtt_gb300 import ops
+    m, n = 1500, 100
+    g = np.random.default_rng(11)
+    s0 = np.concatenate([np.ones(20), np.logspace(-1, -14, 60), np.zeros(20)])
+    U0 = np.linalg.qr(g.standard_normal((m, n)))[0]
+    V0 = np.linalg.qr(g.standard_normal((n, n)))[0]
+    a = (U0 * s0) @ V0.T
+    u, s, vh = ops.svd(t(a, cuda))
+    u, s, vh = u.cpu().numpy(), s.cpu().numpy(), vh.cpu().numpy()
+    assert np.all(np.diff(s) <= 0)
+    assert np.abs(s - s0).max() <= 1e-13
+    assert np.linalg.norm((u * s) @ vh - a) <= 1e-13 * np.linalg.norm(a)
+    assert np.abs(u[:, :80].T @ u[:, :80] - np.eye(80)).max() < 1e-11
+    assert np.abs(vh @ vh.T - np.eye(n)).max() < 1e-12
+
+
 def test_gmres_known_answer(cuda):
     """The reference's GMRES known answer (1-D Laplacian, restart 40, 4 cycles): the device GMRES
     (CGS2) follows the same trajectory as the reference's MGS."""

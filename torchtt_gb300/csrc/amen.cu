@@ -750,6 +750,10 @@ int AmenRun::choose_fp64_engine() {
   if (p_.fp64_engine == 1) return kFp64Native;
   if (p_.fp64_engine == 2) return kFp64DoubleFloat;
   if (!mixed_) return kFp64Native;
+  // Double-float products are accurate to ~1e-13 of the sum of the magnitudes of their terms, so
+  // a residual with cancellation (||A|| ||x|| / ||b|| up to cond(A)) carries ~1e-13 cond(A) of
+  // error: ample at eps >= 1e-9, marginal below (1e-10 on a system of condition 2e3 is within 50x).
+  if (p_.eps < 1e-9) return kFp64Native;
   const int d = d_;
   DBuf nrm((size_t)(2 * d), s_);
   for (int i = 0; i < d; ++i) {

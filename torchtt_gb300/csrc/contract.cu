@@ -11,6 +11,7 @@
 #include <atomic>
 #include <cstdlib>
 #include <mutex>
+#include <shared_mutex>
 #include <type_traits>
 #include <unordered_map>
 
@@ -154,22 +155,25 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams<T> p) {
 // the FP32 pipe is ~60x the FP64 pipe, this is several times the FP64 rate at ~1e-13 relative
 // accuracy (operands within the FP32 exponent range).
 //
-// The split is built from the bits of x with integer operations: h keeps the sign, the exponent
-// and the top 23 stored mantissa bits (truncation), l is the remaining 29 mantissa bits converted
-// to FP32 (round to nearest) and scaled by the exponent, so x = h + l to 2^-47 relative. The obvious
-// form h = (float)x, l = (float)(x - h) runs two conversions and a subtraction on the FP64 pipe for
-// every loaded element; on GB300 that pipe then bounds the kernel (ncu: FP64 pipe 51% active
-// against 31% for the FP32 FMA pipe).
+// The split is built from the bits of x with integer operations: h is x rounded to 24 significant
+// bits (the sign, exponent and top 23 stored mantissa bits, plus one unit when the first dropped
+// bit is set - a carry into the exponent is the correct rounding), l is the signed remainder
+// (|l| <= 2^-24 |h|) converted to FP32 and scaled by the exponent, so x = h + l to 2^-48 relative.
+// The obvious form h = (float)x, l = (float)(x - h) runs two conversions and a subtraction on the
+// FP64 pipe for every loaded element; on GB300 that pipe then bounds the kernel (ncu: FP64 pipe 51%
+// active against 31% for the FP32 FMA pipe).
 __device__ __forceinline__ void df_split(double x, float& h, float& l) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
   const unsigned sign = hi & 0x80000000u;
   const int fe = (int)((hi >> 20) & 0x7ffu) - 896;   // biased FP32 exponent of x (1023 - 127)
   if (fe >= 1 && fe <= 254) {
-    h = __uint_as_float(sign | ((unsigned)fe << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
-    const float r =
-        __uint2float_rn(lo & 0x1fffffffu) * 0x1p-52f * __uint_as_float((unsigned)fe << 23);
-    l = __uint_as_float(__float_as_uint(r) | sign);
+    const unsigned rb = (lo >> 28) & 1u;
+    h = __uint_as_float((sign | ((unsigned)fe << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29)) + rb);
+    // x - h in units of 2^(e - 1075): the 29 dropped bits, less 2^29 when h was rounded up
+    const int rem = (int)(lo & 0x1fffffffu) - (int)(rb << 29);
+    const float r = __int2float_rn(rem) * 0x1p-52f * __uint_as_float((unsigned)fe << 23);
+    l = __uint_as_float(__float_as_uint(r) ^ sign);
   } else if (((hi & 0x7fffffffu) | lo) == 0u) {   // +-0 (also every masked load)
     h = __uint_as_float(sign);
     l = 0.f;
@@ -334,7 +338,7 @@ constexpr TileCfg kCandidates[] = {{64, 64, 0}, {64, 32, 0}, {32, 64, 0}, {32, 3
 constexpr int kNumCandidates = (int)(sizeof(kCandidates) / sizeof(kCandidates[0]));
 
 std::atomic<int> g_autotune{-1};   // -1: not read yet from TTGB_AUTOTUNE
-std::mutex g_tune_mu;
+std::shared_mutex g_tune_mu;   // readers: every launch of a recorded class; writers: tuning
 std::unordered_map<uint64_t, int> g_tune_table;   // class -> candidate index (-1: being tuned)
 std::atomic<int64_t> g_tune_runs{0};
 
@@ -444,7 +448,12 @@ int tuned_choice(const ContractDescT<T>& d, const KParams<T>& p, cudaStream_t st
   if (overlaps<T>(d.C, sc, d.A, sa) || overlaps<T>(d.C, sc, d.B, sb)) return -1;
   const uint64_t key = tune_key(d);
   {
-    std::lock_guard<std::mutex> g(g_tune_mu);
+    std::shared_lock<std::shared_mutex> g(g_tune_mu);
+    auto it = g_tune_table.find(key);
+    if (it != g_tune_table.end()) return it->second;
+  }
+  {
+    std::unique_lock<std::shared_mutex> g(g_tune_mu);
     auto it = g_tune_table.find(key);
     if (it != g_tune_table.end()) return it->second;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -476,7 +485,7 @@ int tuned_choice(const ContractDescT<T>& d, const KParams<T>& p, cudaStream_t st
   cudaEventDestroy(ev[1]);
   g_tune_runs.fetch_add(1);
   {
-    std::lock_guard<std::mutex> g(g_tune_mu);
+    std::unique_lock<std::shared_mutex> g(g_tune_mu);
     g_tune_table[key] = best;
   }
   tuned = true;   // every candidate overwrote C with the full result
@@ -532,7 +541,7 @@ int set_autotune(int mode) {
 }
 
 int64_t autotune_classes() {
-  std::lock_guard<std::mutex> g(g_tune_mu);
+  std::shared_lock<std::shared_mutex> g(g_tune_mu);
   return (int64_t)g_tune_table.size();
 }
 

@@ -8,6 +8,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <utility>
 
 #include "contract.cuh"
 #include "linalg.cuh"
@@ -19,6 +21,12 @@ namespace ttgb {
 namespace {
 
 constexpr double kEps = 2.220446049250313e-16;
+
+// FP32-preconditioned Jacobi for the cluster SVD path (TTGB_SVD_PRECONDITION=0 turns it off).
+const bool g_svd_precondition = [] {
+  const char* e = std::getenv("TTGB_SVD_PRECONDITION");
+  return !(e && e[0] == '0');
+}();
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -459,6 +467,33 @@ __device__ __forceinline__ bool jacobi_rotation(double a, double b, double g, do
   return true;
 }
 
+// FP32 rotation of the preconditioning sweeps (same formulas, all in FP32).
+__device__ __forceinline__ bool jacobi_rotation(float a, float b, float g, float tol, float& c,
+                                                float& s) {
+  if (a == 0.f || b == 0.f) return false;
+  if (!(g * g > tol * tol * a * b)) return false;
+  const float bma = b - a, g2 = 2.f * g;
+  float t;
+  if (fabsf(bma) >= fabsf(g2)) {
+    const float r = __fdividef(g2, bma);
+    t = __fdividef(r, 1.0f + sqrtf(fmaf(r, r, 1.0f)));
+  } else {
+    const float z = __fdividef(bma, g2);
+    t = __fdividef(copysignf(1.0f, z), fabsf(z) + sqrtf(fmaf(z, z, 1.0f)));
+  }
+  if (!isfinite(t)) return false;
+  c = rsqrtf(fmaf(t, t, 1.0f));
+  s = c * t;
+  return true;
+}
+
+__device__ __forceinline__ float warp_sum_t(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum_t(double v) { return warp_sum_d(v); }
+
 __device__ __forceinline__ int rr_index(int p, int r, int nn) {
   return p == 0 ? 0 : ((p - 1 + r) % (nn - 1)) + 1;
 }
@@ -582,60 +617,63 @@ constexpr int kJacobiBlockMaxN = 160;
 // One rotation of a column pair with tracked squared column norms (*na, *nb): only the inner product is
 // reduced; the norms follow the rotation exactly (a' = c^2 a - 2cs g + s^2 b, b' = s^2 a + 2cs g +
 // c^2 b) and are recomputed from the columns once per sweep, which bounds their drift.
-__device__ __forceinline__ int jacobi_rotate_tracked(double* wp, double* wq, double* vp, double* vq,
-                                                     double* na, double* nb, int n, double tol,
-                                                     int lane) {
-  double g = 0.0;
+template <typename T>
+__device__ __forceinline__ int jacobi_rotate_tracked(T* wp, T* wq, T* vp, T* vq, T* na, T* nb, int n,
+                                                     T tol, int lane) {
+  T g = T(0);
   for (int i = lane; i < n; i += 32) g = fma(wp[i], wq[i], g);
-  g = warp_sum_d(g);
-  const double a = *na, b = *nb;
-  double c, s;
+  g = warp_sum_t(g);
+  const T a = *na, b = *nb;
+  T c, s;
   if (!jacobi_rotation(a, b, g, tol, c, s)) return 0;
   for (int i = lane; i < n; i += 32) {
-    const double x = wp[i], y = wq[i];
+    const T x = wp[i], y = wq[i];
     wp[i] = c * x - s * y;
     wq[i] = s * x + c * y;
-    const double u = vp[i], v = vq[i];
+    const T u = vp[i], v = vq[i];
     vp[i] = c * u - s * v;
     vq[i] = s * u + c * v;
   }
   if (lane == 0) {
-    const double cc = c * c, ss = s * s, cs2 = 2.0 * c * s * g;
-    *na = fmax(cc * a - cs2 + ss * b, 0.0);
-    *nb = fmax(ss * a + cs2 + cc * b, 0.0);
+    const T cc = c * c, ss = s * s, cs2 = T(2) * c * s * g;
+    const T a2 = cc * a - cs2 + ss * b, b2 = ss * a + cs2 + cc * b;
+    *na = a2 > T(0) ? a2 : T(0);
+    *nb = b2 > T(0) ? b2 : T(0);
   }
   return 1;
 }
 
+template <typename T>
 __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
-    jacobi_block_kernel(const double* __restrict__ Win, int n, double* Wout, double* Vout,
-                        int max_sweeps, int* status) {
-  extern __shared__ double sm[];
+    jacobi_block_kernel(const T* __restrict__ Win, int n, T* Wout, T* Vout, int max_sweeps,
+                        int* status, const T* __restrict__ Vin) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T* sm = reinterpret_cast<T*>(sm_raw);
   cg::cluster_group cluster = cg::this_cluster();
   constexpr int C = kJacobiCluster, P = 2 * kJacobiCluster;
   const int rank = (int)cluster.block_rank();
   const int nb = (n + P - 1) / P;
-  const int64_t blk = (int64_t)nb * n;   // doubles of one block of W (or of V)
+  const int64_t blk = (int64_t)nb * n;   // elements of one block of W (or of V)
   const int64_t unit = 2 * blk + nb + (nb & 1);   // W block, V block, squared column norms
   // buffer x (0/1), slot s (0/1): W block, V block, norms
-  auto Wb = [&](double* base, int x, int sl) { return base + (int64_t)(x * 2 + sl) * unit; };
-  auto Vb = [&](double* base, int x, int sl) { return base + (int64_t)(x * 2 + sl) * unit + blk; };
-  auto Nb = [&](double* base, int x, int sl) { return base + (int64_t)(x * 2 + sl) * unit + 2 * blk; };
+  auto Wb = [&](T* base, int x, int sl) { return base + (int64_t)(x * 2 + sl) * unit; };
+  auto Vb = [&](T* base, int x, int sl) { return base + (int64_t)(x * 2 + sl) * unit + blk; };
+  auto Nb = [&](T* base, int x, int sl) { return base + (int64_t)(x * 2 + sl) * unit + 2 * blk; };
   __shared__ int counts[kJacobiCluster];
   __shared__ int local_cnt;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  const double tol = fmax((double)n, 1.0) * kEps;
+  const T tol = T(n > 1 ? n : 1) * (sizeof(T) == 8 ? T(kEps) : T(1.1920929e-7f));
   // round 0 of sweep 0: slot 0 holds block rank, slot 1 block P-1-rank
   for (int sl = 0; sl < 2; ++sl) {
     const int b = sl == 0 ? rank : P - 1 - rank;
-    double* W = Wb(sm, 0, sl);
-    double* V = Vb(sm, 0, sl);
+    T* W = Wb(sm, 0, sl);
+    T* V = Vb(sm, 0, sl);
     for (int64_t t = tid; t < blk; t += nt) {
       const int j = (int)(t / n), i = (int)(t - (int64_t)j * n);
       const int c = b * nb + j;
-      W[t] = (c < n) ? Win[(int64_t)c * n + i] : 0.0;
-      V[t] = (c < n && i == c) ? 1.0 : 0.0;
+      W[t] = (c < n) ? Win[(int64_t)c * n + i] : T(0);
+      V[t] = (c < n) ? (Vin ? Vin[(int64_t)c * n + i] : (i == c ? T(1) : T(0))) : T(0);
     }
   }
   int* counts0 = cluster.map_shared_rank(counts, 0);
@@ -645,14 +683,14 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
   __syncthreads();
   while (true) {
     const int bA = rr_index(rank, r, P), bB = rr_index(P - 1 - rank, r, P);
-    double* WA = Wb(sm, x, 0); double* VA = Vb(sm, x, 0); double* NA = Nb(sm, x, 0);
-    double* WB = Wb(sm, x, 1); double* VB = Vb(sm, x, 1); double* NB = Nb(sm, x, 1);
+    T* WA = Wb(sm, x, 0); T* VA = Vb(sm, x, 0); T* NA = Nb(sm, x, 0);
+    T* WB = Wb(sm, x, 1); T* VB = Vb(sm, x, 1); T* NB = Nb(sm, x, 1);
     if (r == 0) {   // fresh column norms, then the pairs inside each block, once per sweep
       for (int c = warp; c < 2 * nb; c += nw) {
-        const double* w = (c < nb ? WA : WB) + (int64_t)(c % nb) * n;
-        double a = 0.0;
+        const T* w = (c < nb ? WA : WB) + (int64_t)(c % nb) * n;
+        T a = T(0);
         for (int i = lane; i < n; i += 32) a = fma(w[i], w[i], a);
-        a = warp_sum_d(a);
+        a = warp_sum_t(a);
         if (lane == 0) (c < nb ? NA : NB)[c % nb] = a;
       }
       __syncthreads();
@@ -663,9 +701,9 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
           int p = rr_index(pi, t, m2), q = rr_index(m2 - 1 - pi, t, m2);
           if (p > q) { const int u = p; p = q; q = u; }
           if (q >= nb) continue;
-          double* W = sl ? WB : WA;
-          double* V = sl ? VB : VA;
-          double* Nm = sl ? NB : NA;
+          T* W = sl ? WB : WA;
+          T* V = sl ? VB : VA;
+          T* Nm = sl ? NB : NA;
           mine += jacobi_rotate_tracked(W + (int64_t)p * n, W + (int64_t)q * n, V + (int64_t)p * n,
                                         V + (int64_t)q * n, Nm + p, Nm + q, n, tol, lane);
         }
@@ -676,11 +714,11 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
       for (int j = warp; j < nb; j += nw) {
         const int k = (j + t) % nb;
         const int ga = bA * nb + j, gb = bB * nb + k;
-        double *wp = WA + (int64_t)j * n, *wq = WB + (int64_t)k * n;
-        double *vp = VA + (int64_t)j * n, *vq = VB + (int64_t)k * n;
-        double *np = NA + j, *nq = NB + k;
+        T *wp = WA + (int64_t)j * n, *wq = WB + (int64_t)k * n;
+        T *vp = VA + (int64_t)j * n, *vq = VB + (int64_t)k * n;
+        T *np = NA + j, *nq = NB + k;
         if (ga > gb) {
-          double* u = wp; wp = wq; wq = u; u = vp; vp = vq; vq = u; u = np; np = nq; nq = u;
+          T* u = wp; wp = wq; wq = u; u = vp; vp = vq; vq = u; u = np; np = nq; nq = u;
         }
         mine += jacobi_rotate_tracked(wp, wq, vp, vq, np, nq, n, tol, lane);
       }
@@ -710,12 +748,12 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
         if (rr_index(c, r, P) == b) { owner = c; oslot = 0; }
         if (rr_index(P - 1 - c, r, P) == b) { owner = c; oslot = 1; }
       }
-      const double* srcW = cluster.map_shared_rank(Wb(sm, x, oslot), owner);
-      const double* srcV = cluster.map_shared_rank(Vb(sm, x, oslot), owner);
-      const double* srcN = cluster.map_shared_rank(Nb(sm, x, oslot), owner);
-      double* dW = Wb(sm, 1 - x, sl);
-      double* dV = Vb(sm, 1 - x, sl);
-      double* dN = Nb(sm, 1 - x, sl);
+      const T* srcW = cluster.map_shared_rank(Wb(sm, x, oslot), owner);
+      const T* srcV = cluster.map_shared_rank(Vb(sm, x, oslot), owner);
+      const T* srcN = cluster.map_shared_rank(Nb(sm, x, oslot), owner);
+      T* dW = Wb(sm, 1 - x, sl);
+      T* dV = Vb(sm, 1 - x, sl);
+      T* dN = Nb(sm, 1 - x, sl);
       for (int64_t t = tid; t < blk; t += nt) { dW[t] = srcW[t]; dV[t] = srcV[t]; }
       for (int t = tid; t < nb; t += nt) dN[t] = srcN[t];
     }
@@ -723,12 +761,12 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
     x = 1 - x;
     r = rn;
   }
-  if (rank == 0 && tid == 0 && !converged) *status = 3;
+  if (rank == 0 && tid == 0 && !converged && status) *status = 3;
   // buffer x holds the blocks of round r
   for (int sl = 0; sl < 2; ++sl) {
     const int b = rr_index(sl == 0 ? rank : P - 1 - rank, r, P);
-    const double* W = Wb(sm, x, sl);
-    const double* V = Vb(sm, x, sl);
+    const T* W = Wb(sm, x, sl);
+    const T* V = Vb(sm, x, sl);
     for (int64_t t = tid; t < blk; t += nt) {
       const int j = (int)(t / n), i = (int)(t - (int64_t)j * n);
       const int c = b * nb + j;
@@ -794,6 +832,15 @@ __global__ void __launch_bounds__(256) jacobi_grid_round_kernel(double* W, doubl
     __syncthreads();
   }
   if (lane == 0 && mine) atomicAdd(count, (unsigned)mine);
+}
+
+// out = (float)(W / nrm) (zero when the norm is zero)
+__global__ void cast_scaled_kernel(const double* __restrict__ W, const double* __restrict__ nrm,
+                                   float* out, int64_t total) {
+  const double sc = nrm[0] > 0.0 ? 1.0 / nrm[0] : 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x)
+    out[t] = (float)(W[t] * sc);
 }
 
 __global__ void identity_kernel(double* V, int n) {
@@ -1108,9 +1155,40 @@ void svd(const double* A, int64_t lda, int64_t m, int64_t n, double* U, double* 
   DBuf Up((size_t)(n * n), s);   // U' (normalised columns of the rotated R^T, sorted)
   if (n <= kJacobiBlockMaxN && n >= 2 * kJacobiCluster) {
     const int nb = (int)((n + 2 * kJacobiCluster - 1) / (2 * kJacobiCluster));
-    const size_t smem = (size_t)4 * (2 * nb * n + nb + (nb & 1)) * sizeof(double);
-    smem_optin((const void*)jacobi_block_kernel, (int)smem);
-    jacobi_block_kernel<<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status);
+    const int64_t unit = 2 * nb * n + nb + (nb & 1);
+    const double* Vin = nullptr;
+    if (g_svd_precondition) {
+      // FP32 sweeps first (Frobenius-normalised copy), then the FP64 sweeps start from their
+      // rotations made orthogonal to FP64 rounding: the FP64 Jacobi (the same kernel, the same
+      // stopping rule, so the same accuracy) then only finishes what FP32 could not resolve.
+      const size_t smem32 = (size_t)4 * unit * sizeof(float);
+      smem_optin((const void*)jacobi_block_kernel<float>, (int)smem32);
+      DBuf nrm(1, s), Vp((size_t)(n * n), s), G((size_t)(n * n), s), T((size_t)(n * n), s);
+      FBuf W32((size_t)(n * n), s), V32((size_t)(n * n), s);
+      nrm2(red, W, n * n, nrm.p, s);
+      cast_scaled_kernel<<<cdiv(n * n, 256), 256, 0, s>>>(W, nrm.p, W32.p, n * n);
+      TTGB_CHECK_LAUNCH();
+      jacobi_block_kernel<float><<<kJacobiCluster, 256, smem32, s>>>(W32.p, (int)n, W32.p, V32.p,
+                                                                      30, nullptr, nullptr);
+      TTGB_CHECK_LAUNCH();
+      cast(V32.p, Vp.p, n * n, s);
+      // Newton-Schulz polar iteration V <- V (3 I - V^T V) / 2: quadratic from the FP32
+      // orthogonality (~1e-5) to FP64 rounding in three steps, all on the contraction engine
+      for (int it = 0; it < 3; ++it) {
+        gemm_cm(Vp.p, n, Vp.p, n, G.p, n, n, n, n, 1.0, 0.0, s, true, false);   // G = V^T V
+        copy(Vp.p, T.p, n * n, s);
+        gemm_cm(Vp.p, n, G.p, n, T.p, n, n, n, n, -0.5, 1.5, s);                 // T = 1.5 V - 0.5 V G
+        std::swap(Vp.p, T.p);
+      }
+      gemm_cm(W, n, Vp.p, n, G.p, n, n, n, n, 1.0, 0.0, s);                     // W V
+      copy(G.p, W, n * n, s);
+      copy(Vp.p, Vw + n * n, n * n, s);
+      Vin = Vw + n * n;
+    }
+    const size_t smem = (size_t)4 * unit * sizeof(double);
+    smem_optin((const void*)jacobi_block_kernel<double>, (int)smem);
+    jacobi_block_kernel<double><<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status,
+                                                                  Vin);
     TTGB_CHECK_LAUNCH();
     DBuf sig((size_t)n, s);
     svd_sort_kernel<<<1, 1024, 0, s>>>(W, Vw, (int)n, Up.p, S, Vw + n * n, sig.p);
@@ -1151,8 +1229,11 @@ void svd(const double* A, int64_t lda, int64_t m, int64_t n, double* U, double* 
   const size_t smem = (size_t)2 * n * n * sizeof(double);
   const int use_smem = smem <= 200 * 1024 ? 1 : 0;
   if (use_smem) smem_optin((const void*)jacobi_svd_kernel, (int)smem);
-  jacobi_svd_kernel<<<1, 512, use_smem ? smem : 0, s>>>(W, Vw, (int)n, Up.p, S, use_smem, 60,
-                                                         ws.status, nullptr);
+  // one warp per column pair of a round (n < 2 * kJacobiCluster here): idle warps would only
+  // lengthen every block barrier of the round-robin sweep
+  const int threads = (int)std::min<int64_t>(512, 32 * std::max<int64_t>(1, (n + 1) / 2));
+  jacobi_svd_kernel<<<1, threads, use_smem ? smem : 0, s>>>(W, Vw, (int)n, Up.p, S, use_smem, 60,
+                                                             ws.status, nullptr);
   TTGB_CHECK_LAUNCH();
   // U = Q V'
   gemm_cm(Qb.p, m, Vw, n, U, m, m, n, n, 1.0, 0.0, s);
