@@ -8,8 +8,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <cstdlib>
-#include <utility>
 
 #include "contract.cuh"
 #include "linalg.cuh"
@@ -21,12 +19,6 @@ namespace ttgb {
 namespace {
 
 constexpr double kEps = 2.220446049250313e-16;
-
-// FP32-preconditioned Jacobi for the cluster SVD path (TTGB_SVD_PRECONDITION=0 turns it off).
-const bool g_svd_precondition = [] {
-  const char* e = std::getenv("TTGB_SVD_PRECONDITION");
-  return !(e && e[0] == '0');
-}();
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -467,31 +459,6 @@ __device__ __forceinline__ bool jacobi_rotation(double a, double b, double g, do
   return true;
 }
 
-// FP32 rotation of the preconditioning sweeps (same formulas, all in FP32).
-__device__ __forceinline__ bool jacobi_rotation(float a, float b, float g, float tol, float& c,
-                                                float& s) {
-  if (a == 0.f || b == 0.f) return false;
-  if (!(g * g > tol * tol * a * b)) return false;
-  const float bma = b - a, g2 = 2.f * g;
-  float t;
-  if (fabsf(bma) >= fabsf(g2)) {
-    const float r = __fdividef(g2, bma);
-    t = __fdividef(r, 1.0f + sqrtf(fmaf(r, r, 1.0f)));
-  } else {
-    const float z = __fdividef(bma, g2);
-    t = __fdividef(copysignf(1.0f, z), fabsf(z) + sqrtf(fmaf(z, z, 1.0f)));
-  }
-  if (!isfinite(t)) return false;
-  c = rsqrtf(fmaf(t, t, 1.0f));
-  s = c * t;
-  return true;
-}
-
-__device__ __forceinline__ float warp_sum_t(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 __device__ __forceinline__ double warp_sum_t(double v) { return warp_sum_d(v); }
 
 __device__ __forceinline__ int rr_index(int p, int r, int nn) {
@@ -609,7 +576,8 @@ __global__ void __launch_bounds__(512) jacobi_svd_kernel(double* Wg, double* Vg,
 // pair of columns is visited once per sweep, as in the scalar cyclic order, with one cluster
 // barrier per round (P - 1 per sweep), and every dot product reads local memory. The sweep's
 // rotation count is summed in CTA 0 after a barrier and read by every CTA, so all CTAs leave the
-// loop together.
+// loop together. The value type T is the arithmetic of the sweeps; Vin (optional) gives starting
+// rotations (identity when null), Vout the accumulated ones.
 // ---------------------------------------------------------------------------------------------
 constexpr int kJacobiCluster = 8;
 constexpr int kJacobiBlockMaxN = 160;
@@ -832,15 +800,6 @@ __global__ void __launch_bounds__(256) jacobi_grid_round_kernel(double* W, doubl
     __syncthreads();
   }
   if (lane == 0 && mine) atomicAdd(count, (unsigned)mine);
-}
-
-// out = (float)(W / nrm) (zero when the norm is zero)
-__global__ void cast_scaled_kernel(const double* __restrict__ W, const double* __restrict__ nrm,
-                                   float* out, int64_t total) {
-  const double sc = nrm[0] > 0.0 ? 1.0 / nrm[0] : 0.0;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x)
-    out[t] = (float)(W[t] * sc);
 }
 
 __global__ void identity_kernel(double* V, int n) {
@@ -1156,39 +1115,10 @@ void svd(const double* A, int64_t lda, int64_t m, int64_t n, double* U, double* 
   if (n <= kJacobiBlockMaxN && n >= 2 * kJacobiCluster) {
     const int nb = (int)((n + 2 * kJacobiCluster - 1) / (2 * kJacobiCluster));
     const int64_t unit = 2 * nb * n + nb + (nb & 1);
-    const double* Vin = nullptr;
-    if (g_svd_precondition) {
-      // FP32 sweeps first (Frobenius-normalised copy), then the FP64 sweeps start from their
-      // rotations made orthogonal to FP64 rounding: the FP64 Jacobi (the same kernel, the same
-      // stopping rule, so the same accuracy) then only finishes what FP32 could not resolve.
-      const size_t smem32 = (size_t)4 * unit * sizeof(float);
-      smem_optin((const void*)jacobi_block_kernel<float>, (int)smem32);
-      DBuf nrm(1, s), Vp((size_t)(n * n), s), G((size_t)(n * n), s), T((size_t)(n * n), s);
-      FBuf W32((size_t)(n * n), s), V32((size_t)(n * n), s);
-      nrm2(red, W, n * n, nrm.p, s);
-      cast_scaled_kernel<<<cdiv(n * n, 256), 256, 0, s>>>(W, nrm.p, W32.p, n * n);
-      TTGB_CHECK_LAUNCH();
-      jacobi_block_kernel<float><<<kJacobiCluster, 256, smem32, s>>>(W32.p, (int)n, W32.p, V32.p,
-                                                                      30, nullptr, nullptr);
-      TTGB_CHECK_LAUNCH();
-      cast(V32.p, Vp.p, n * n, s);
-      // Newton-Schulz polar iteration V <- V (3 I - V^T V) / 2: quadratic from the FP32
-      // orthogonality (~1e-5) to FP64 rounding in three steps, all on the contraction engine
-      for (int it = 0; it < 3; ++it) {
-        gemm_cm(Vp.p, n, Vp.p, n, G.p, n, n, n, n, 1.0, 0.0, s, true, false);   // G = V^T V
-        copy(Vp.p, T.p, n * n, s);
-        gemm_cm(Vp.p, n, G.p, n, T.p, n, n, n, n, -0.5, 1.5, s);                 // T = 1.5 V - 0.5 V G
-        std::swap(Vp.p, T.p);
-      }
-      gemm_cm(W, n, Vp.p, n, G.p, n, n, n, n, 1.0, 0.0, s);                     // W V
-      copy(G.p, W, n * n, s);
-      copy(Vp.p, Vw + n * n, n * n, s);
-      Vin = Vw + n * n;
-    }
     const size_t smem = (size_t)4 * unit * sizeof(double);
     smem_optin((const void*)jacobi_block_kernel<double>, (int)smem);
     jacobi_block_kernel<double><<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status,
-                                                                  Vin);
+                                                                  nullptr);
     TTGB_CHECK_LAUNCH();
     DBuf sig((size_t)n, s);
     svd_sort_kernel<<<1, 1024, 0, s>>>(W, Vw, (int)n, Up.p, S, Vw + n * n, sig.p);
