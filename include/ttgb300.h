@@ -268,7 +268,10 @@ int ttgb_calibrate_fma(int32_t dtype, double* tflops);
    strides, device) that overwrites its output times every tile shape with and without split-K on
    the caller's stream and keeps the fastest for the process. mode 1 turns it on (the default
    unless the environment sets TTGB_AUTOTUNE=0), 0 off (occupancy heuristic), any other value only
-   queries; returns the previous state. ttgb_autotune_classes gives the number of recorded classes. */
+   queries; returns the previous state. ttgb_autotune_classes gives the number of recorded classes.
+   When the environment sets TTGB_AUTOTUNE_TABLE to a file path, the records of earlier processes
+   are read from it at the first contraction and every new record is appended ("class candidate"
+   lines), so a restarted server or a profiler run reuses the tuned tiles without timing them. */
 int ttgb_autotune(int32_t mode);
 int64_t ttgb_autotune_classes(void);
 

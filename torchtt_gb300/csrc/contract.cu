@@ -9,7 +9,9 @@
 #include <climits>
 
 #include <atomic>
+#include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <mutex>
 #include <shared_mutex>
 #include <type_traits>
@@ -341,6 +343,31 @@ std::atomic<int> g_autotune{-1};   // -1: not read yet from TTGB_AUTOTUNE
 std::shared_mutex g_tune_mu;   // readers: every launch of a recorded class; writers: tuning
 std::unordered_map<uint64_t, int> g_tune_table;   // class -> candidate index (-1: being tuned)
 std::atomic<int64_t> g_tune_runs{0};
+std::once_flag g_table_once;
+std::string g_table_path;   // TTGB_AUTOTUNE_TABLE: records read at first use, new ones appended
+
+// Reads "class candidate" lines (hex, decimal) of a previous process into the table.
+void load_table() {
+  const char* e = std::getenv("TTGB_AUTOTUNE_TABLE");
+  if (!e || !*e) return;
+  std::unique_lock<std::shared_mutex> g(g_tune_mu);
+  g_table_path = e;
+  FILE* f = std::fopen(e, "r");
+  if (!f) return;
+  unsigned long long k = 0;
+  int c = 0;
+  while (std::fscanf(f, "%llx %d", &k, &c) == 2)
+    if (c >= 0 && c < kNumCandidates) g_tune_table[(uint64_t)k] = c;
+  std::fclose(f);
+}
+
+void append_record(uint64_t key, int c) {   // caller holds the unique lock
+  if (g_table_path.empty() || c < 0) return;
+  FILE* f = std::fopen(g_table_path.c_str(), "a");
+  if (!f) return;
+  std::fprintf(f, "%llx %d\n", (unsigned long long)key, c);
+  std::fclose(f);
+}
 
 bool autotune_on() {
   int v = g_autotune.load();
@@ -419,8 +446,6 @@ void launch_tiles(const ContractDescT<T>& d, KParams<T> p, int bm, int bn, int s
 
 template <typename T>
 uint64_t tune_key(const ContractDescT<T>& d) {
-  int dev = 0;
-  cudaGetDevice(&dev);
   const int eng = std::is_same<T, float>::value ? 2 : (t_fp64_engine == kFp64DoubleFloat ? 1 : 0);
   const int units = (d.am.s0 == 1) | ((d.ak.s0 == 1) << 1) | ((d.bk.s0 == 1) << 2) |
                     ((d.bn.s0 == 1) << 3) | ((d.cm.s0 == 1) << 4);
@@ -431,7 +456,7 @@ uint64_t tune_key(const ContractDescT<T>& d) {
   k = k * 64 + (uint64_t)log2_bucket(d.batch);
   k = k * 4 + (uint64_t)(d.tri & 3);
   k = k * 32 + (uint64_t)units;
-  k = k * 64 + (uint64_t)(dev & 63);
+  k = k * 1024 + (uint64_t)(num_sms() & 1023);   // the GPU model, through its SM count
   return k;
 }
 
@@ -446,6 +471,7 @@ int tuned_choice(const ContractDescT<T>& d, const KParams<T>& p, cudaStream_t st
   const int64_t sb = (d.batch - 1) * d.b_bs + ax_span(d.bk, d.K) + ax_span(d.bn, d.N);
   const int64_t sc = (d.batch - 1) * d.c_bs + ax_span(d.cm, d.M) + ax_span(d.cn, d.N);
   if (overlaps<T>(d.C, sc, d.A, sa) || overlaps<T>(d.C, sc, d.B, sb)) return -1;
+  std::call_once(g_table_once, load_table);
   const uint64_t key = tune_key(d);
   {
     std::shared_lock<std::shared_mutex> g(g_tune_mu);
@@ -487,6 +513,7 @@ int tuned_choice(const ContractDescT<T>& d, const KParams<T>& p, cudaStream_t st
   {
     std::unique_lock<std::shared_mutex> g(g_tune_mu);
     g_tune_table[key] = best;
+    append_record(key, best);
   }
   tuned = true;   // every candidate overwrote C with the full result
   return best;
