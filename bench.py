@@ -360,6 +360,21 @@ def run_gb300(args):
         "share_of_solve": pm["lowp_ms"] / max(1e-9, sum(pm["phase_ms"].values())),
     })
     fp64_tflops = pf["contract_flops"] / (pf["contract_ms"] * 1e-3) / 1e12 if pf["contract_ms"] > 0 else None
+    # Krylov orthogonalisation (multidot + two gs_update per GMRES iteration) against HBM: the
+    # reference's algorithmic bytes 8 N_loc (2k + 3) per iteration / the kernels' event time, and
+    # the bytes the CGS2 kernels actually move; the basis (<= 41 vectors of N_loc doubles, ~125 MB
+    # at the largest local problem) is mostly L2-resident, so HBM is an upper bound of the rate
+    kms = pm.get("krylov_ms", 0.0)
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    kry = {"kernels": "multidot_kernel + 2x gs_update_kernel per GMRES iteration (mixed path)",
+           "bound": "hbm", "unit": "GB/s", "peak": hbm,
+           "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks
+                          else "fallback 6.8 TB/s",
+           "achieved": pm["krylov_bytes"] / (kms * 1e-3) / 1e9 if kms > 0 else None,
+           "moved_gbs": pm["krylov_traffic_bytes"] / (kms * 1e-3) / 1e9 if kms > 0 else None,
+           "ms": kms, "launches": pm.get("krylov_launches"),
+           "avg_launch_us": 1000 * kms / max(1, pm.get("krylov_launches", 0))}
+    kry["frac"] = kry["achieved"] / hbm if kry["achieved"] else None
     fp64_roof = {"kernel": "contract_kernel<double> (FP64 contraction engine, plain path)",
                  "achieved": fp64_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
                  "frac": fp64_tflops / fp64_peak if fp64_tflops else None,
@@ -423,6 +438,7 @@ def run_gb300(args):
             "server": {"peak_running": srv_stats.get("peak_running"), "completed": srv_stats.get("completed")},
             "roofline": roofline,
             "fp64_contract_roofline": fp64_roof,
+            "krylov_roofline": kry,
             "phase_ms_mixed": pm["phase_ms"],
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": h2d,

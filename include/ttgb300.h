@@ -109,6 +109,12 @@ typedef struct ttgb_stats {
   double lowp_ms;               /* profile + mixed: device time of the low-precision products */
   int64_t lowp_launches;        /* profile + mixed: kernel launches of those products */
   double lowp_gemm_flops;       /* profile + mixed: flops of their GEMM launches */
+  double krylov_ms;             /* profile: device time of the GMRES orthogonalisation kernels */
+  int64_t krylov_launches;      /* profile: their launches */
+  double krylov_bytes;          /* profile: algorithmic bytes of those iterations, 8 N_loc (2k + 3)
+                                   for iteration k (the reference's MGS reads k + 1 vectors twice
+                                   and writes one) */
+  double krylov_traffic_bytes;  /* profile: bytes the CGS2 kernels read and write, 8 N_loc (4k + 10) */
 } ttgb_stats;
 
 typedef struct ttgb_solution ttgb_solution;   /* opaque, library-owned result */

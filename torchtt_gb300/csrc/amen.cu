@@ -107,6 +107,7 @@ class AmenRun {
     if (p.profile) {
       prof_.reset(new Profiler(s_));
       prof_lowp_.reset(new Profiler(s_));
+      prof_krylov_.reset(new Profiler(s_));
       phases_.reset(new PhaseTimer(s_));
     }
   }
@@ -147,6 +148,7 @@ class AmenRun {
   AmenStats st_;
   std::unique_ptr<Profiler> prof_;
   std::unique_ptr<Profiler> prof_lowp_;
+  std::unique_ptr<Profiler> prof_krylov_;
   int64_t op_count_ = 0;   // applications of the current local operator
   int64_t lowp_count_ = 0; // low-precision applications of the current local operator
   bool mixed_ = false;
@@ -535,6 +537,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
     op.w1 = w1_.p;
     op.w2 = w2_.p;
     op.prof = prof_.get();
+    op.prof_krylov = prof_krylov_.get();
     op_count_ = 0;
     op.count = &op_count_;
     if (p_.prec != kNoPrec) {
@@ -920,6 +923,11 @@ AmenResult AmenRun::run(const TTView& x0, const TTView& z0) {
     st_.lowp_ms = prof_lowp_->ms;
     st_.lowp_launches = prof_lowp_->launches;
     st_.lowp_gemm_flops = prof_lowp_->flops;
+    prof_krylov_->flush();
+    st_.krylov_ms = prof_krylov_->ms;
+    st_.krylov_launches = prof_krylov_->launches;
+    st_.krylov_bytes = prof_krylov_->flops;
+    st_.krylov_traffic_bytes = prof_krylov_->aux;
   }
   res.stats = st_;
   return res;

@@ -67,6 +67,12 @@ struct AmenStats {
   double lowp_ms = 0.0;
   int64_t lowp_launches = 0;
   double lowp_gemm_flops = 0.0;   // flops of their GEMM launches
+  // profile only: CUDA-event time of the GMRES orthogonalisation kernels, the reference's
+  // algorithmic bytes of those iterations (8 N_loc (2k + 3)) and the bytes the kernels move
+  double krylov_ms = 0.0;
+  int64_t krylov_launches = 0;
+  double krylov_bytes = 0.0;
+  double krylov_traffic_bytes = 0.0;
   // filled when AmenParams::profile is set: CUDA-event time of the contraction launches and the
   // flops of their GEMMs (an A stage run from the nonzeros of a sparse core is not counted)
   double contract_ms = 0.0;

@@ -210,6 +210,10 @@ int ttgb_solution_stats(const ttgb_solution* sol, ttgb_stats* st) {
     st->lowp_ms = a.lowp_ms;
     st->lowp_launches = a.lowp_launches;
     st->lowp_gemm_flops = a.lowp_gemm_flops;
+    st->krylov_ms = a.krylov_ms;
+    st->krylov_launches = a.krylov_launches;
+    st->krylov_bytes = a.krylov_bytes;
+    st->krylov_traffic_bytes = a.krylov_traffic_bytes;
   });
 }
 
@@ -518,6 +522,6 @@ int ttgb_calibrate_fma(int32_t dtype, double* tflops) {
   });
 }
 
-int32_t ttgb_version(void) { return 100; }
+int32_t ttgb_version(void) { return 101; }
 
 }  // extern "C"

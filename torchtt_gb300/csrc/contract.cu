@@ -488,7 +488,14 @@ int tuned_choice(const ContractDescT<T>& d, const KParams<T>& p, cudaStream_t st
     g_tune_table[key] = -1;   // being tuned: other threads use the heuristic meanwhile
   }
   const int sms = num_sms();
-  cudaEvent_t ev[2];
+  struct Events {   // destroyed on every exit, also when a launch check throws
+    cudaEvent_t e[2] = {nullptr, nullptr};
+    ~Events() {
+      if (e[0]) cudaEventDestroy(e[0]);
+      if (e[1]) cudaEventDestroy(e[1]);
+    }
+  } evs;
+  cudaEvent_t* ev = evs.e;
   TTGB_CUDA(cudaEventCreate(&ev[0]));
   TTGB_CUDA(cudaEventCreate(&ev[1]));
   int best = -1;
@@ -507,8 +514,6 @@ int tuned_choice(const ContractDescT<T>& d, const KParams<T>& p, cudaStream_t st
       if (rep == 1 && (best < 0 || ms < best_ms)) { best = c; best_ms = ms; }
     }
   }
-  cudaEventDestroy(ev[0]);
-  cudaEventDestroy(ev[1]);
   g_tune_runs.fetch_add(1);
   {
     std::unique_lock<std::shared_mutex> g(g_tune_mu);

@@ -160,9 +160,12 @@ GmresResult gmres(const LocalOperator& op, const double* rhs, double* sol, int i
       double* qk = Q + (int64_t)k * n;
       double* w = Q + (int64_t)(k + 1) * n;
       op.apply(qk, w, true, s);
+      if (op.prof_krylov) op.prof_krylov->begin();
       multidot(red, Q, n, k + 1, w, n, h1, s);
       gs_update(red, Q, n, k + 1, h1, w, n, h2, true, false, s);
       gs_update(red, Q, n, k + 1, h2, w, n, &scal[2], false, true, s);
+      if (op.prof_krylov)
+        op.prof_krylov->end(8.0 * (double)n * (2 * k + 3), 3, 8.0 * (double)n * (4 * k + 10));
       gmres_step_kernel<<<1, 32, 0, s>>>(k, iters, h1, h2, scal, H, cs, sn, beta, threshold,
                                          ws.d_flag);
       TTGB_CHECK_LAUNCH();

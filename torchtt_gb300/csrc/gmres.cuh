@@ -54,6 +54,10 @@ struct LocalOperator {
   float* w2f = nullptr;
   TcLocal* tc = nullptr;        // when set, the low-precision engine is the tcgen05 3xTF32 GEMM
   Profiler* prof_lowp = nullptr;  // optional timing of the low-precision products
+  // optional timing of the Krylov orthogonalisation of each GMRES iteration; its first figure is
+  // the reference's algorithmic bytes 8 N_loc (2k + 3) of iteration k (k + 1 basis vectors), the
+  // second the bytes the CGS2 kernels read and write, 8 N_loc (4k + 10)
+  Profiler* prof_krylov = nullptr;
   int64_t* count_lowp = nullptr;
   int64_t size() const { return dims.r * dims.n * dims.R; }
   void apply(const double* x, double* y, bool use_prec, cudaStream_t s) const;

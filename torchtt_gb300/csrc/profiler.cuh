@@ -13,11 +13,13 @@ struct Profiler {
   cudaStream_t s = nullptr;
   std::vector<cudaEvent_t> pool;
   std::vector<double> pending_flops;
+  std::vector<double> pending_aux;
   std::vector<int> pending_launches;
   size_t used = 0;
   double ms = 0.0;
   int64_t launches = 0;
-  double flops = 0.0;
+  double flops = 0.0;   // the first work figure of every bracket (flops or bytes)
+  double aux = 0.0;     // an optional second figure
 
   explicit Profiler(cudaStream_t st, size_t pairs = 2048) : s(st) {
     pool.resize(2 * pairs);
@@ -33,9 +35,10 @@ struct Profiler {
     if (used + 2 > pool.size()) flush();
     TTGB_CUDA(cudaEventRecord(pool[used], s));
   }
-  void end(double f, int nlaunch) {
+  void end(double f, int nlaunch, double f2 = 0.0) {
     TTGB_CUDA(cudaEventRecord(pool[used + 1], s));
     pending_flops.push_back(f);
+    pending_aux.push_back(f2);
     pending_launches.push_back(nlaunch);
     used += 2;
   }
@@ -48,8 +51,10 @@ struct Profiler {
       ms += t;
     }
     for (double f : pending_flops) flops += f;
+    for (double f : pending_aux) aux += f;
     for (int l : pending_launches) launches += l;
     pending_flops.clear();
+    pending_aux.clear();
     pending_launches.clear();
     used = 0;
   }
