@@ -51,3 +51,28 @@ def test_sm103a_only(built):
     """The shared object carries sm_103a code (cuobjdump is not used: the ELF notes list the arch)."""
     from torchtt_gb300 import build
     assert "arch=compute_103a,code=sm_103a" in " ".join(build.ARCH)
+
+
+def test_ctypes_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of ttgb_tt, ttgb_amen_params and ttgb_stats have the C compiler's size and
+    field offsets (a binding with a stale layout would read or overrun the wrong bytes)."""
+    import ctypes
+    from torchtt_gb300 import _lib
+    mirrors = {"ttgb_tt": _lib.TTDesc, "ttgb_amen_params": _lib.AmenParams, "ttgb_stats": _lib.Stats}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "ttgb300.h"', "int main(void) {"]
+    for cname, cls in mirrors.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in cls._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {" ".join(ln.split()[:2]): int(ln.split()[2]) for ln in out if ln.strip()}
+    for cname, cls in mirrors.items():
+        assert got[cname + " size"] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got["%s %s" % (cname, f)] == getattr(cls, f).offset, (cname, f)

@@ -103,7 +103,8 @@ def run(workload="laplace_potential_d20_n64", batch=8, slots=8, precision="mixed
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="laplace_potential_d20_n64")
+    ap.add_argument("--workload", default="laplace_potential_d20_n64",
+                    choices=["laplace_potential_d20_n64", "laplace_d8_n16"])
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
