@@ -3,7 +3,9 @@
 //
 // GB300 note: FP64 runs at ~1.9 FMA/clock/SM (measured), so every O(m n^2) step is expressed as a
 // GEMM on the contraction engine (spread over all SMs); only O(n^3) steps on the small n x n
-// factors (Cholesky, triangular inverse, Jacobi) run inside one thread block.
+// factors run on few SMs: Cholesky + triangular inverse and the Jacobi of n < 16 in one thread
+// block, the block Jacobi of 16 <= n <= 160 on an 8-CTA cluster, larger ones one grid-wide round
+// per launch. Small QRs (the kickrank-wide blocks) run a shared-memory Householder in one block.
 #include <cooperative_groups.h>
 
 #include <algorithm>
