@@ -3,9 +3,11 @@
 // The kernel is a shared-memory-tiled FP64 GEMM (BMxBN output tile, BK=16, 256 threads, each
 // thread a (BM/16)x(BN/16) register tile). Every operand index may be a pair of tensor indices with
 // their own strides (struct Ax), so the reference's tensordot permutes (cpp/amen_solve.h:17-98)
-// cost no copies. FP64 FMA throughput is the bound on this path; the tile shape is picked per call
-// so that the grid covers the SMs, and split-K (atomic FP64 adds) is used when even the smallest
-// tile leaves SMs idle.
+// cost no copies. FP64 FMA throughput is the bound on this path. The tile shape and split-K
+// (atomic FP64 adds) of a launch come from the tile autotuner's record for its shape class, or
+// from an occupancy heuristic: the largest tile whose grid covers the SMs, split-K when even the
+// smallest tile leaves SMs idle. The same engine runs in double-float arithmetic on the FP32 pipe
+// (contract_df_kernel) and in FP32.
 #include <climits>
 
 #include <atomic>
