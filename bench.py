@@ -23,9 +23,10 @@ Synthetic seeded data; no dataset is involved.
   path batched, the relative residual of every solution and ||x_mixed - x_fp64|| / ||x_fp64||.
   ``e2e`` repeats batched steps with host-resident (pinned) inputs through the public API, so the
   host-to-device copies of A and every b_j and the copies of the solutions back are timed.
-* reference arm: the reference's CPU algorithm (the numpy restatement in oracle/, on all host
-  threads; the compiled reference is not available on the GPU host) on rank 0 only, one solve of
-  the same workload per step.
+* reference arm: the reference's own CPU implementation (its package ``torchtt`` installed in
+  baseline/_ref, with its C++ extension compiled on this host from the reference's sources by
+  oracle/build_ref.py; ``torchtt.solvers.amen_solve(use_cpp=True)``, FP64, all host threads) on
+  rank 0 only, one solve of the same workload per step.
 """
 import argparse
 import json
@@ -160,6 +161,63 @@ def cpu_solve_once(wl):
     return time.perf_counter() - t0, info
 
 
+def reference_solver():
+    """The reference's own CPU implementation of the path: its package ``torchtt`` from the install
+    in baseline/_ref with the C++ extension ``torchttcpp`` compiled for this host from the
+    reference's sources (oracle/build_ref.py). Returns ``(solve(wl) -> seconds, kind, how)``.
+
+    ``torchtt.solvers.amen_solve(A, b, ..., use_cpp=True)`` is called when the package imports
+    (its public API, which calls ``torchttcpp.amen_solve``, torchtt/solvers.py:268-285); when its
+    Python dependencies are missing on this host, ``torchttcpp.amen_solve`` is called with the
+    arguments that function passes. Where the reference cannot be built, the numpy restatement
+    of its algorithm (oracle/amen.py) is timed instead and reported as kind "port"."""
+    import torch
+    torch.set_num_threads(os.cpu_count() or 1)
+    try:
+        from oracle import build_ref
+        torchtt, cpp = build_ref.load_installed()
+    except Exception as e:  # noqa: BLE001 - reported in the JSON line
+        why = str(e).strip().splitlines()[0] if str(e).strip() else type(e).__name__
+
+        def solve_port(wl):
+            return cpu_solve_once(wl)[0]
+        return solve_port, "port", ("the numpy restatement of the reference (oracle/amen.py); the "
+                                    "compiled reference is unavailable here: %s" % why)
+
+    def args_of(wl):
+        p = wl["params"]
+        return dict(nswp=p.get("nswp", 22), eps=p["eps"], kickrank=p["kickrank"])
+
+    if torchtt is not None:
+        def solve_api(wl):
+            kw = args_of(wl)
+            A, b = torchtt.TT(list(wl["A"])), torchtt.TT(list(wl["b"]))
+            torch.manual_seed(1)
+            t0 = time.perf_counter()
+            torchtt.solvers.amen_solve(A, b, use_cpp=True, **kw)
+            return time.perf_counter() - t0
+        return solve_api, "reference", ("torchtt.solvers.amen_solve(use_cpp=True) of the reference's "
+                                        "install (baseline/_ref), its C++ extension compiled on this "
+                                        "host from the reference's sources")
+
+    def solve_ext(wl):
+        kw = args_of(wl)
+        A, b = list(wl["A"]), list(wl["b"])
+        d = len(A)
+        N = [int(c.shape[2]) for c in A]
+        rA = [1] + [int(c.shape[3]) for c in A]
+        rb = [1] + [int(c.shape[2]) for c in b]
+        torch.manual_seed(1)
+        t0 = time.perf_counter()
+        cpp.amen_solve(A, b, [], N, rA, rb, [1] * (d + 1), kw["nswp"], kw["eps"], 32768, 500,
+                       kw["kickrank"], 0, 40, 2, False, 0)
+        return time.perf_counter() - t0
+    return solve_ext, "reference", ("torchttcpp.amen_solve (cpp/amen_solve.h:122) compiled on this host "
+                                    "from the reference's sources, called with the arguments of "
+                                    "torchtt/solvers.py:283 (the package's Python dependencies are "
+                                    "not installed here)")
+
+
 def workload_config(args, wl):
     p = wl["params"]
     return {"workload": args.workload, "d": len(wl["A"]), "n": int(wl["A"][0].shape[1]),
@@ -167,30 +225,42 @@ def workload_config(args, wl):
             "eps": p["eps"], "kickrank": p["kickrank"], "nswp": p.get("nswp", 22)}
 
 
+def arm_config(args, wl, ws):
+    """The ``config`` of the JSON line, the same for both arms."""
+    cfg = workload_config(args, wl)
+    cfg.update({"precision": "mixed", "engine": args.engine, "batch": args.batch,
+                "server_slots": args.slots, "l2": "256 MiB flush write between steps",
+                "parallelism": "replicas" if ws > 1 else "single"})
+    return cfg
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     cores = os.cpu_count() or 1
+    solve, kind, how = reference_solver()
     times = []
     for i in range(args.warmup + args.steps):
         wl = get_workload(args.workload, args.seed + i % args.batch)
-        dt, info = cpu_solve_once(wl)
+        dt = solve(wl)
         if i >= args.warmup:
             times.append(dt)
     total = sum(times)
     value = len(times) / total
-    cfg = workload_config(args, get_workload(args.workload, args.seed))
-    cfg.update({"precision": "fp64", "batch": 1, "l2": "host run"})
     line = {
         "metric": METRIC, "impl": "reference", "value": value, "unit": "solves/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded)", "config": cfg,
+        "data": "synthetic (seeded)",
+        "config": arm_config(args, get_workload(args.workload, args.seed), ws),
+        "reference_path": "plain FP64 on the host CPU, one solve per step (the reference has no "
+                          "mixed-precision or batched path); right-hand side of step i: seed "
+                          "%d + i mod %d" % (args.seed, args.batch),
         "latency_ms": {"p50": 1000 * percentile(times, 0.5), "p99": 1000 * percentile(times, 0.99)},
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": "%d full solves of %s (one per step), numpy/OpenBLAS on all host "
-                                   "threads" % (len(times), args.workload)},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": kind,
+                         "sample": "%d full solves of %s (one per step), %s, torch intra-op threads = "
+                                   "%d" % (len(times), args.workload, how, cores)},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -412,10 +482,7 @@ def run_gb300(args):
                          % (args.workload, seeds[0])}
 
     if rank == 0:
-        cfg = workload_config(args, wls[0])
-        cfg.update({"precision": "mixed", "engine": engine, "batch": nb, "server_slots": args.slots,
-                    "l2": "256 MiB flush write between steps",
-                    "parallelism": "replicas" if ws > 1 else "single"})
+        cfg = arm_config(args, wls[0], ws)
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,

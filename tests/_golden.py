@@ -21,5 +21,24 @@ def params(z):
     return {k[2:]: z[k].item() for k in z.files if k.startswith("p_")}
 
 
-def solve_fixtures():
-    return sorted(f for f in os.listdir(GOLDEN) if f.startswith("solve_") and f.endswith(".npz"))
+def is_sampled(z):
+    """A fixture that summarises the reference's solution by sampled entries (large workloads)."""
+    return "sample_x" in z.files
+
+
+def solve_fixtures(kind="all", max_cpp_s=None):
+    """Whole-solve fixtures: ``kind`` "full" (the reference's solution cores stored), "sampled"
+    (its solution summarised by sampled entries, norm, ranks and residual) or "all"; with
+    ``max_cpp_s`` only those whose reference solve took at most that many seconds."""
+    out = []
+    for f in sorted(os.listdir(GOLDEN)):
+        if not (f.startswith("solve_") and f.endswith(".npz")):
+            continue
+        z = load(f)
+        sampled = is_sampled(z)
+        if kind == "full" and sampled or kind == "sampled" and not sampled:
+            continue
+        if max_cpp_s is not None and float(z["t_cpp"]) > max_cpp_s:
+            continue
+        out.append(f)
+    return out

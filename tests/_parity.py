@@ -45,3 +45,56 @@ def dense_cond(A_cores):
     mat = t.transpose(perm).reshape(int(np.prod(M)), int(np.prod(N)))
     s = np.linalg.svd(mat, compute_uv=False)
     return float(s[0] / s[-1])
+
+
+def tt_entries(cores, idx):
+    """Entries x(i_1, .., i_d) of a TT-vector at the rows of ``idx`` (S x d)."""
+    cores = [np.asarray(c) for c in cores]
+    idx = np.asarray(idx, dtype=np.int64)
+    v = cores[0][0, idx[:, 0], :]
+    for k in range(1, len(cores)):
+        v = np.einsum("sr,srR->sR", v, np.transpose(cores[k][:, idx[:, k], :], (1, 0, 2)))
+    return v[:, 0]
+
+
+def sampled_relerr(x, z):
+    """Estimate of ||x - x_ref|| / ||x_ref|| from the reference's entries at uniformly drawn
+    multi-indices (tests/golden/make_golden.py: sampled_case): the ratio of the sampled
+    root-mean-square difference to the sampled root-mean-square of x_ref. Both means estimate
+    the squared norms divided by the number of entries, without bias."""
+    ref = np.asarray(z["sample_x"])
+    got = tt_entries(x, z["sample_idx"])
+    return float(np.sqrt(np.mean((got - ref) ** 2)) / np.sqrt(np.mean(ref ** 2)))
+
+
+def res_bound(eps, res_ref):
+    """Residual bar: eps where the reference reaches eps on the same input, else twice the
+    reference's own residual (its stopping rule is the local residual, cpp/amen_solve.h:375,525,
+    so its true residual can exceed eps)."""
+    return eps if res_ref <= eps else 2.0 * res_ref
+
+
+def check_sampled(A, b, x, z, eps, kickrank, label="", err_bound=None):
+    """Parity of a solution against a sampled fixture of the reference's: relative residual
+    (oracle TT algebra) within ``res_bound``, the TT norm within 10 eps of the reference's, the
+    sampled estimate of ||x - x_ref|| / ||x_ref|| within 10 eps (or ``err_bound``), TT ranks within
+    +-kickrank."""
+    A = [np.asarray(a) for a in A]
+    b = [np.asarray(c) for c in b]
+    x = [np.asarray(c) for c in x]
+    res = O.tt_relres(A, x, b)
+    res_ref = float(z["ref_relres"])
+    nrm, nrm_ref = O.tt_norm(x), float(z["ref_norm"])
+    err = sampled_relerr(x, z)
+    ranks = [c.shape[0] for c in x] + [1]
+    ranks_ref = [int(r) for r in z["ref_ranks"]]
+    eb = 10 * eps if err_bound is None else err_bound
+    msg = "%s res %.3e (ref %.3e, bar %.3e) sampled err %.3e (bar %.3e) norm %.12e (ref %.12e) " \
+          "ranks %s ref %s" % (label, res, res_ref, res_bound(eps, res_ref), err, eb, nrm, nrm_ref,
+                               ranks, ranks_ref)
+    print(msg)
+    assert res <= res_bound(eps, res_ref), msg
+    assert abs(nrm - nrm_ref) <= 10 * eps * nrm_ref, msg
+    assert err <= eb, msg
+    assert all(abs(a - c) <= kickrank for a, c in zip(ranks, ranks_ref)), msg
+    return res, res_ref, err

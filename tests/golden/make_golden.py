@@ -229,9 +229,109 @@ def solve_case(torchtt, cpp, wl, seed, prec=None, with_python=False, extra=None)
     print("solve_%s.npz written (cpp %.2fs)" % (name, t_cpp))
 
 
+def tt_entries(cores, idx):
+    """Entries x(i_1, .., i_d) of a TT-vector at the rows of ``idx`` (S x d), by a batched chain of
+    row-vector x core-slice products."""
+    cores = [c.numpy() if torch.is_tensor(c) else np.asarray(c) for c in cores]
+    v = cores[0][0, idx[:, 0], :]                                  # S x r1
+    for k in range(1, len(cores)):
+        sl = np.transpose(cores[k][:, idx[:, k], :], (1, 0, 2))    # S x r x R
+        v = np.einsum("sr,srR->sR", v, sl)
+    return v[:, 0]
+
+
+def sampled_case(torchtt, cpp, wl, seed, name, nsamples=4096):
+    """A whole solve at a size whose solution is too large to store (tens of MB at d = 20): the
+    inputs, the parameters, the initial enrichment cores z0 that the reference draws with
+    ``torch::randn`` after ``torch.manual_seed(seed)``, and a summary of the solution
+    ``torchttcpp.amen_solve`` (``cpp/amen_solve.h:122``) returns:
+
+    * its TT ranks and Frobenius norm, and its relative residual ||A x - b|| / ||b|| (oracle TT
+      algebra);
+    * its entries at ``nsamples`` multi-indices drawn uniformly from the full index space. For a
+      second solution y of the same system, N mean_i (y(i) - x(i))^2 is an unbiased estimate of
+      ||y - x||^2 (N the number of entries), so the sampled root-mean-square difference over the
+      sampled root-mean-square of x estimates ||y - x|| / ||x|| without storing x."""
+    from oracle import amen as O
+    A, b, x0 = wl["A"], wl["b"], wl.get("x0")
+    p = dict(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
+             local_iterations=40, resets=2)
+    p.update(wl["params"])
+    d = len(A)
+    N = [c.shape[2] for c in A]
+    rA = [1] + [c.shape[3] for c in A]
+    rb = [1] + [c.shape[2] for c in b]
+    torch.manual_seed(seed)
+    rz = [1] + [p["kickrank"] + p["kick2"]] * (d - 1) + [1]
+    z0 = [torch.randn(rz[i], N[i], rz[i + 1], dtype=torch.float64) for i in range(d)]
+    torch.manual_seed(seed)
+    t0 = time.time()
+    xr = cpp.amen_solve(A, b, [], N, rA, rb, [1] * (d + 1), p["nswp"], p["eps"], p["rmax"],
+                        p["max_full"], p["kickrank"], p["kick2"], p["local_iterations"],
+                        p["resets"], False, 0)
+    t_cpp = time.time() - t0
+    xs = [c.numpy() for c in xr]
+    An, bn = [c.numpy() for c in A], [c.numpy() for c in b]
+    g = np.random.Generator(np.random.PCG64(seed + 9176))
+    idx = np.stack([g.integers(0, n, size=nsamples) for n in N], axis=1).astype(np.int64)
+    out = {}
+    _pack_cores("A", A, out)
+    _pack_cores("b", b, out)
+    _pack_cores("z0", z0, out)
+    for k, v in p.items():
+        out["p_" + k] = np.array(v)
+    out["prec"] = np.array(0)
+    out["seed"] = np.array(seed)
+    out["t_cpp"] = np.array(t_cpp)
+    out["threads"] = np.array(torch.get_num_threads())
+    out["ref_ranks"] = np.array([c.shape[0] for c in xs] + [1], dtype=np.int64)
+    out["ref_norm"] = np.array(O.tt_norm(xs))
+    out["ref_relres"] = np.array(O.tt_relres(An, xs, bn))
+    out["sample_idx"] = idx.astype(np.uint8 if max(N) <= 256 else np.int32)
+    out["sample_x"] = tt_entries(xs, idx)
+    np.savez_compressed(os.path.join(HERE, "solve_%s.npz" % name), **out)
+    print("solve_%s.npz written (cpp %.2fs, ranks <= %d, relres %.3e)"
+          % (name, t_cpp, max(out["ref_ranks"]), float(out["ref_relres"])), flush=True)
+
+
+def rounding_case(torchtt, cpp):
+    """Rounding stress d=16 n=32 (A = Laplacian + C C^T + I), the right-hand side (a sum of 4
+    random TTs) rounded to 1e-8 by the reference's own TT.round (torchtt/_tt_base.py:1427) before
+    the solve. With the full terms of rank 16 (input rank 64) the reference's solve stops after 20
+    sweeps at relres 0.70 with ranks <= 161 (AMEn grows a rank by at most kickrank per sweep, and
+    this solution needs far more), so the fixture uses terms of rank 4 (input rank 16) and nswp 40,
+    where it converges."""
+    wl = W.rounding_stress(0, term_rank=4, nswp=40)
+    bt = torchtt.TT(list(wl["b"])).round(wl["round_b"])
+    wl = dict(wl, b=[c.contiguous() for c in bt.cores])
+    sampled_case(torchtt, cpp, wl, 40, "rounding_stress_d16_n32_sys0_r16")
+
+
+def large_solves(torchtt, cpp):
+    """Sampled fixtures of the benchmark workloads at their full sizes: the d=20 n=64 solve of the
+    benchmark (its first right-hand side), one system of each batch workload, and two requests of
+    the serving trace."""
+    sampled_case(torchtt, cpp, W.laplace_potential_d20_n64(2), 2, "laplace_potential_d20_n64")
+    # parametric diffusion d=10 n=32: system 13 (rhs rank 1) and system 3 (rhs rank 15)
+    for i in (13, 3):
+        wl = W.parametric_diffusion_d10_n32(i)
+        sampled_case(torchtt, cpp, wl, 30 + i, "parametric_diffusion_d10_n32_sys%d_r%d" % (i, wl["rhs_rank"]))
+    rounding_case(torchtt, cpp)
+    # serving trace requests: 44 (d=24, n=64, rank 8, eps 1e-8), 14 (d=20, n=32, rank 5, eps 1e-10)
+    for i in (44, 14):
+        wl = W.serving_request(i)
+        sampled_case(torchtt, cpp, wl, 50 + i, "serving_req%d_d%d_n%d" % (i, wl["d"], wl["n"]))
+
+
 def main():
     torch.set_num_threads(max(1, os.cpu_count() or 1))
     torchtt, cpp = build_ref.load_reference_package()
+    if len(sys.argv) > 1 and sys.argv[1] == "large":
+        large_solves(torchtt, cpp)
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "rounding":
+        rounding_case(torchtt, cpp)
+        return
     kernels(torchtt)
     rounding(torchtt)
     division(torchtt)

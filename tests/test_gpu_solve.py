@@ -15,6 +15,16 @@ def to_dev(cores, dev):
     return [torch.from_numpy(np.ascontiguousarray(c)).to(dev) for c in cores]
 
 
+def _check(z, A, b, xs, p, label):
+    """Full fixtures: the solution against the reference's cores; sampled fixtures (the benchmark
+    workloads at full size): residual, norm, ranks and the sampled estimate of ||x - x_ref||."""
+    if G.is_sampled(z):
+        _parity.check_sampled(A, b, xs, z, p["eps"], p["kickrank"], label=label)
+        return
+    cond = _parity.dense_cond(A) if int(np.prod([a.shape[1] for a in A])) <= 2000 else None
+    _parity.check(A, b, xs, G.cores(z, "x_cpp"), p["eps"], p["kickrank"], cond=cond, label=label)
+
+
 @pytest.mark.parametrize("fixture", G.solve_fixtures())
 def test_solve_matches_reference(cuda, fixture):
     from torchtt_gb300 import TT, amen_solve
@@ -29,8 +39,7 @@ def test_solve_matches_reference(cuda, fixture):
                        kick2=p["kick2"], local_iterations=p["local_iterations"], resets=p["resets"],
                        preconditioner=prec, z0=to_dev(z0, cuda), return_stats=True)
     xs = [c.cpu().numpy() for c in x.cores]
-    cond = _parity.dense_cond(A) if int(np.prod([a.shape[1] for a in A])) <= 2000 else None
-    _parity.check(A, b, xs, G.cores(z, "x_cpp"), p["eps"], p["kickrank"], cond=cond, label=fixture)
+    _check(z, A, b, xs, p, fixture)
     assert st["sweeps"] >= 1 and st["local_solves"] > 0
 
 
@@ -92,9 +101,7 @@ def test_mixed_solve_matches_reference(cuda, fixture):
                        preconditioner=prec, z0=to_dev(z0, cuda), return_stats=True,
                        precision="mixed")
     xs = [c.cpu().numpy() for c in x.cores]
-    cond = _parity.dense_cond(A) if int(np.prod([a.shape[1] for a in A])) <= 2000 else None
-    _parity.check(A, b, xs, G.cores(z, "x_cpp"), p["eps"], p["kickrank"], cond=cond,
-                  label=fixture + " mixed")
+    _check(z, A, b, xs, p, fixture + " mixed")
 
 
 def test_mixed_equals_fp64_on_laplace(cuda):

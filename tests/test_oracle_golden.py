@@ -34,7 +34,7 @@ def test_gmres_known_answer():
     assert np.linalg.norm(x - xr) <= 1e-10 * np.linalg.norm(xr)
 
 
-@pytest.mark.parametrize("fixture", G.solve_fixtures())
+@pytest.mark.parametrize("fixture", G.solve_fixtures("full") + G.solve_fixtures("sampled", max_cpp_s=2.0))
 def test_oracle_solve_matches_reference(fixture):
     z = G.load(fixture)
     A, b = G.cores(z, "A"), G.cores(z, "b")
@@ -44,6 +44,9 @@ def test_oracle_solve_matches_reference(fixture):
                            max_full=p["max_full"], kickrank=p["kickrank"], kick2=p["kick2"],
                            local_iterations=p["local_iterations"], resets=p["resets"],
                            prec=int(z["prec"]), z0=z0)
+    if G.is_sampled(z):
+        _parity.check_sampled(A, b, x, z, p["eps"], p["kickrank"], label=fixture)
+        return
     cond = _parity.dense_cond(A) if int(np.prod([a.shape[1] for a in A])) <= 2000 else None
     _parity.check(A, b, x, G.cores(z, "x_cpp"), p["eps"], p["kickrank"], cond=cond, label=fixture)
     if G.cores(z, "x_py") is not None:   # the reference's Python path agrees with its C++ path
