@@ -408,6 +408,7 @@ def run_gb300(args):
             "flops": "algorithmic (dense local-product count) per product / product time",
             "gemm_tflops": gemm_tflops,
             "traffic": read_profile_value("tc_gemm_d20_n64_local.md", "traffic_bytes_per_launch"),
+            "traffic_source": "profiles/tc_gemm_d20_n64_local.md (one ncu capture, per launch)",
             "kernel": "low-precision local product: tc_gemm_kernel (tcgen05.mma kind::tf32, 3xTF32 "
                       "split) for its GEMMs + structured A stage + operand split",
             "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
@@ -451,6 +452,8 @@ def run_gb300(args):
                  "peak_source": "FP64 FMA pipe measured live (ttgb_calibrate_fma)",
                  "traffic": read_profile_value("contract_f64_laplace_potential_d20_n64.md",
                                                "traffic_bytes_per_launch"),
+                 "traffic_source": "profiles/contract_f64_laplace_potential_d20_n64.md (one ncu "
+                                   "capture, per launch)",
                  "launches": pf["contract_launches"],
                  "avg_launch_us": 1000 * pf["contract_ms"] / max(1, pf["contract_launches"])}
 
@@ -458,7 +461,7 @@ def run_gb300(args):
     A_h = TT([c.clone().pin_memory() for c in wls[0]["A"]])
     bs_h = [TT([c.clone().pin_memory() for c in w["b"]]) for w in wls]
     h2d = nb * sum(c.numel() * 8 for c in A_h.cores) + sum(c.numel() * 8 for b in bs_h for c in b.cores)
-    e2e_steps = max(1, min(args.steps, 2))
+    e2e_steps = args.steps
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d2h = 0

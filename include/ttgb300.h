@@ -160,8 +160,21 @@ int ttgb_server_wait(ttgb_server* srv, int64_t id, double timeout_s, ttgb_soluti
 /* Server counters: requests submitted, completed, running now, peak concurrently running. */
 int ttgb_server_stats(const ttgb_server* srv, int64_t* submitted, int64_t* completed,
                       int32_t* running, int32_t* peak_running);
+/* Admission accounting: the server's budget, the bytes reserved by the running requests now and
+ * the most reserved at once so far. Each request reserves its ttgb_footprint bound. */
+int ttgb_server_memory(const ttgb_server* srv, int64_t* budget, int64_t* in_use,
+                       int64_t* peak_in_use);
 /* Finishes queued and running requests, then frees the server. */
 void ttgb_server_destroy(ttgb_server* srv);
+/* Upper bound of the device bytes one solve of A x = b with these parameters allocates (the
+ * server's admission unit): every core, interface and local workspace at the largest TT rank the
+ * solve can reach, rank(x0) + nswp (kickrank + kick2), capped by rmax and by the mode sizes.
+ * x0 may be NULL. (no reference counterpart: the reference has no admission) */
+int ttgb_footprint(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0,
+                   const ttgb_amen_params* params, int64_t* bytes);
+/* Bytes the library's stream-ordered allocations hold in the current device's default memory
+ * pool now and at most since the last reset (reset_high != 0 resets the high-water mark). */
+int ttgb_pool_usage(int64_t* used_now, int64_t* used_high, int32_t reset_high);
 
 /* ---- TT-level operations (FP64, device cores; a TT-matrix when x->rows is set) ---- */
 
@@ -222,7 +235,9 @@ int ttgb_local_product_lowp(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t
  * 4194304 (larger requests return TTGB_ERR_INVALID with a message in ttgb_last_error()). The first
  * call on a device looks up the array's device address (cudaGetSymbolAddress) with that device
  * current; make that first call before any stream capture. All calls share the array: calls that
- * overlap on the GPU race and must be ordered by the caller. */
+ * overlap on the GPU race and must be ordered by the caller. It always contracts A densely (no
+ * structured A stage), runs no tile-tuning measurements (so it never blocks the host), and does
+ * not support cudaDeviceReset (the array's address is cached per device for the process). */
 int ttgb_local_product_noalloc(int64_t rl, int64_t s, int64_t r, int64_t m, int64_t n, int64_t S,
                                int64_t RL, int64_t R, const double* phi_l, const double* A,
                                const double* phi_r, const double* x, double* y, int32_t nrhs,

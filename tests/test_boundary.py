@@ -67,3 +67,30 @@ def test_tt_algebra_needs_gpu():
         A @ x
     with pytest.raises(RuntimeError):
         b.round(1e-8)
+
+
+def test_torch_operator_schema_and_no_cpu_fallback():
+    """torch.ops.torchtt_gb300.amen_solve is registered with the documented schema and refuses
+    CPU tensors (no CPU fallback)."""
+    import torchtt_gb300  # noqa: F401
+    from torchtt_gb300 import custom_op
+    op = torch.ops.torchtt_gb300.amen_solve
+    assert str(op.default._schema) == "torchtt_gb300::" + custom_op.SCHEMA
+    A, b = small()
+    with pytest.raises(RuntimeError, match="CUDA tensors only"):
+        op(A.cores, b.cores, None)
+
+
+def test_minimal_foreign_tt_argument_checks():
+    """A TT class with only .cores and .is_ttm passes the argument checks (mode sizes are read from
+    the cores) and is rejected with the reference's exceptions when the shapes disagree."""
+    class Bare:
+        def __init__(self, cores):
+            self.cores = cores
+            self.is_ttm = cores[0].dim() == 4
+    A, b = small()
+    from torchtt_gb300 import solvers as S
+    assert S._rows(Bare(A.cores)) == [4, 5, 6] and S._cols(Bare(b.cores)) == [4, 5, 6]
+    wrong = Bare(W.laplace_ttm(3, 4))
+    with pytest.raises(ShapeMismatch):
+        amen_solve(wrong, Bare(b.cores))

@@ -11,6 +11,11 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
+def _dev(cores, dev):
+    from torchtt_gb300 import TT
+    return TT([c.to(dev) for c in cores])
+
+
 def requests(dev):
     from torchtt_gb300 import TT, workloads as W
     out = []
@@ -65,3 +70,31 @@ def test_invalid_request_is_rejected(cuda):
     with Server(slots=2) as srv:
         with pytest.raises(Exception):
             srv.submit(A, b)
+
+
+def test_admission_never_overcommits_on_rank_growth(cuda):
+    """Parametric diffusion systems with rank-16 right-hand sides grow their solution ranks to
+    ~160 (from an initial rank of 1). Each request reserves its footprint bound, so with a budget
+    just above one request's bound the requests run one at a time and the reservations never exceed
+    the budget; the library's actual allocations of a request stay within its bound."""
+    from torchtt_gb300 import workloads as W
+    from torchtt_gb300.serving import Server, footprint, pool_usage
+    wls = [W.parametric_diffusion_d10_n32(3, rhs_rank=16), W.parametric_diffusion_d10_n32(7, rhs_rank=16)]
+    sys = [(_dev(w["A"], cuda), _dev(w["b"], cuda), w["params"]) for w in wls]
+    fps = [footprint(A, b, precision="mixed", **p) for A, b, p in sys]
+    budget = int(1.05 * max(fps))
+    torch.cuda.synchronize()
+    pool_usage(reset_high=True)
+    base_now, _ = pool_usage()
+    with Server(slots=2, mem_budget_bytes=budget) as srv:
+        ids = [srv.submit(A, b, precision="mixed", seed=i, **p) for i, (A, b, p) in enumerate(sys)]
+        res = [srv.result(i) for i in ids]
+        mem = srv.memory()
+        st = srv.stats()
+    _, high = pool_usage()
+    assert mem["budget"] == budget and mem["peak_in_use"] <= budget, mem
+    assert st["peak_running"] == 1, st
+    assert high - base_now <= max(fps), (high, base_now, fps)
+    for (A, b, p), (x, _) in zip(sys, res):
+        assert max(x.R) > 100      # the ranks did grow far beyond the right-hand side's
+        assert float((A @ x - b).norm() / b.norm()) <= 10 * p["eps"]

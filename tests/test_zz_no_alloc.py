@@ -46,6 +46,25 @@ def test_noalloc_matches_allocating_entry_point(cuda, shapes):
         assert float((y - y_ref).abs().max()) <= 1e-12 * scale
 
 
+def test_noalloc_matches_on_a_sparse_laplace_core(cuda):
+    """On a Kronecker-sum Laplacian core ttgb_local_product applies A from its nonzeros (the
+    structured A stage) while the no-allocation variant contracts it densely: same product."""
+    from torchtt_gb300 import _lib, workloads as W
+    L = _lib.lib()
+    A = W.laplace_potential_ttm(4, 64)[1].to(cuda)       # 3 x 64 x 64 x 3, tridiagonal blocks
+    s, n, S = A.shape[0], A.shape[1], A.shape[3]
+    for call, (r, R) in enumerate([(40, 48), (12, 9)]):
+        g = np.random.default_rng(300 + call)
+        mk = lambda *sh: torch.from_numpy(g.standard_normal(sh)).to(cuda)
+        PhiL, PhiR, x = mk(r, s, r), mk(R, S, R), mk(r, n, R)
+        y_ref = torch.empty((r, n, R), dtype=torch.float64, device=cuda)
+        y = torch.full((r, n, R), float("nan"), dtype=torch.float64, device=cuda)
+        assert _call(L.ttgb_local_product, PhiL, A, PhiR, x, y_ref) == 0
+        assert _call(L.ttgb_local_product_noalloc, PhiL, A, PhiR, x, y) == 0, L.ttgb_last_error()
+        torch.cuda.synchronize()
+        assert float((y - y_ref).abs().max()) <= 1e-12 * float(y_ref.abs().max())
+
+
 def test_noalloc_rejects_oversize(cuda):
     from torchtt_gb300 import _lib
     L = _lib.lib()
@@ -55,3 +74,8 @@ def test_noalloc_rejects_oversize(cuda):
     st = L.ttgb_local_product_noalloc(r, s, r, n, n, S, R, R, p, p, p, p, p, 1, None)
     assert st == _lib.TTGB_ERR_INVALID
     assert b"more than the" in L.ttgb_last_error()
+    # dimensions whose scratch size wraps around 2^64 are refused, not truncated
+    big = 1 << 40
+    st = L.ttgb_local_product_noalloc(big, 3, 1, big, 1, 3, 1, big, p, p, p, p, p, 1, None)
+    assert st == _lib.TTGB_ERR_INVALID
+    assert b"more than" in L.ttgb_last_error()

@@ -12,6 +12,7 @@ from .solvers import amen_solve
 from .division import amen_divide
 from .dmrg import dmrg_matvec
 from .amen_mv import amen_mm, amen_mv
+from . import custom_op  # registers torch.ops.torchtt_gb300.amen_solve
 
 __all__ = ["TT", "amen_solve", "amen_divide", "dmrg_matvec", "amen_mv", "amen_mm", "solvers", "errors", "GB300Error", "IncompatibleTypes",
            "InvalidArguments", "RankMismatch", "ShapeMismatch"]

@@ -102,6 +102,11 @@ _SIGS = {
     "ttgb_calibrate_fma": (c_i32, [c_i32, ctypes.POINTER(c_dbl)]),
     "ttgb_last_error": (ctypes.c_char_p, []),
     "ttgb_version": (c_i32, []),
+    "ttgb_server_memory": (c_i32, [c_vp, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64),
+                                   ctypes.POINTER(c_i64)]),
+    "ttgb_footprint": (c_i32, [ctypes.POINTER(TTDesc), ctypes.POINTER(TTDesc), ctypes.POINTER(TTDesc),
+                               ctypes.POINTER(AmenParams), ctypes.POINTER(c_i64)]),
+    "ttgb_pool_usage": (c_i32, [ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), c_i32]),
 }
 
 EXPORTED = tuple(_SIGS)

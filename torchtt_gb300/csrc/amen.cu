@@ -2,6 +2,7 @@
 // tensor in HBM and every arithmetic step a kernel of this library. The host keeps only ranks,
 // the norm bookkeeping scalars (normA/normb/normx/nrmsc, amen_solve.h:195-204) and the stopping
 // decisions; it reads device scalars in small batches (one synchronisation per group of norms).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -934,6 +935,46 @@ AmenResult AmenRun::run(const TTView& x0, const TTView& z0) {
 }
 
 }  // namespace
+
+int64_t max_reachable_rank(const TTView& A, const TTView& x0, const AmenParams& p) {
+  const int d = A.d;
+  int64_t r0 = 1;
+  if (x0.d == d)
+    for (int k = 0; k <= d; ++k) r0 = std::max<int64_t>(r0, x0.ranks[k]);
+  const double grow = (double)r0 + (double)p.nswp * (double)(p.kickrank + p.kick2);
+  double best = 1.0;
+  // mode-size cap of bond k (between cores k-1 and k): min(prod_{i<k} n_i, prod_{i>=k} n_i)
+  for (int k = 1; k < d; ++k) {
+    double left = 1.0, right = 1.0;
+    for (int i = 0; i < k; ++i) left *= (double)A.cols[i];
+    for (int i = k; i < d; ++i) right *= (double)A.cols[i];
+    best = std::max(best, std::min(std::min(left, right), grow));
+  }
+  return (int64_t)std::min<double>(best, (double)p.rmax);
+}
+
+size_t footprint_bound(const TTView& A, const TTView& b, const TTView& x0, const AmenParams& p) {
+  int64_t nmax = 1, smax = 1, rbmax = 1;
+  for (int k = 0; k < A.d; ++k) {
+    nmax = std::max<int64_t>(nmax, A.cols[k]);
+    smax = std::max<int64_t>(smax, A.ranks[k + 1]);
+    rbmax = std::max<int64_t>(rbmax, b.ranks[k + 1]);
+  }
+  const double r = (double)max_reachable_rank(A, x0, p);
+  const double rz = (double)(p.kickrank + p.kick2) + 1.0;
+  const double core = r * r * (double)nmax;                  // one solution core
+  // per core: x, the previous x during a step, z; interfaces Phi (r s r), Phiz (rz s r), Phi_b
+  // (rb r), Phiz_b (rb rz)
+  const double per_core = 2.0 * core + rz * r * (double)nmax + (r * r + rz * r) * (double)smax +
+                          (double)rbmax * (r + rz);
+  // local working set of the largest core: Krylov basis, contraction intermediates (x s, S sides),
+  // mixed-path FP32/TF32 split copies, supercore SVD/QR (matrix, U, V, Gram) and vectors
+  const double nloc = core;
+  const double local = (double)(p.local_iterations + 1) * nloc + 2.0 * nloc * (double)smax +
+                       2.0 * nloc * (double)smax /* split copies, 2 x FP32 */ + 6.0 * nloc +
+                       4.0 * r * r + 16.0 * nloc;
+  return (size_t)(8.0 * ((double)A.d * per_core + local)) + ((size_t)64 << 20);
+}
 
 void randn(double* out, int64_t n, uint64_t seed, uint64_t offset, cudaStream_t s) {
   if (n <= 0) return;

@@ -91,6 +91,15 @@ struct AmenResult {
 AmenResult amen_solve(const TTView& A, const TTView& b, const TTView& x0, const TTView& z0,
                       const AmenParams& p, cudaStream_t stream);
 
+// Upper bound of the device bytes one solve allocates: cores of x and z, the four kinds of
+// interface and the local working set (Krylov basis, contraction intermediates, dense linear
+// algebra) at the largest TT rank the solve can reach. An AMEn sweep raises a rank by at most
+// kickrank + kick2 (the enrichment columns appended to the truncated supercore), so after nswp
+// sweeps a rank is at most rank(x0) + nswp (kickrank + kick2), capped by rmax and by the products
+// of the mode sizes on either side of the bond.
+int64_t max_reachable_rank(const TTView& A, const TTView& x0, const AmenParams& p);
+size_t footprint_bound(const TTView& A, const TTView& b, const TTView& x0, const AmenParams& p);
+
 // device RNG: out[i] ~ N(0,1) from (seed, offset + i)
 void randn(double* out, int64_t n, uint64_t seed, uint64_t offset, cudaStream_t s);
 

@@ -522,6 +522,34 @@ int ttgb_calibrate_fma(int32_t dtype, double* tflops) {
   });
 }
 
+int ttgb_footprint(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0,
+                   const ttgb_amen_params* params, int64_t* bytes) {
+  return guarded([&] {
+    TTGB_REQUIRE(A && b && params && bytes, "null argument");
+    const TTView vA = view_of(A, true), vb = view_of(b, false), vx = view_of(x0, false);
+    TTGB_REQUIRE(vA.d >= 1 && vA.d == vb.d, "Dimension mismatch.");
+    *bytes = (int64_t)footprint_bound(vA, vb, vx, params_from_c(params));
+  });
+}
+
+int ttgb_pool_usage(int64_t* used_now, int64_t* used_high, int32_t reset_high) {
+  return guarded([&] {
+    int dev = 0;
+    TTGB_CUDA(cudaGetDevice(&dev));
+    cudaMemPool_t pool;
+    TTGB_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    unsigned long long cur = 0, high = 0;   // the attributes are 64-bit unsigned
+    TTGB_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &cur));
+    TTGB_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &high));
+    if (used_now) *used_now = (int64_t)cur;
+    if (used_high) *used_high = (int64_t)high;
+    if (reset_high) {
+      unsigned long long zero = 0;
+      TTGB_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero));
+    }
+  });
+}
+
 int32_t ttgb_version(void) { return 101; }
 
 }  // extern "C"

@@ -383,6 +383,8 @@ void append_record(uint64_t key, int c) {   // caller holds the unique lock
   std::fclose(f);
 }
 
+thread_local bool t_no_tuning_runs = false;   // set by NoTuningScope
+
 bool autotune_on() {
   int v = g_autotune.load();
   if (v < 0) {
@@ -496,6 +498,7 @@ int tuned_choice(const ContractDescT<T>& d, const KParams<T>& p, cudaStream_t st
     std::unique_lock<std::shared_mutex> g(g_tune_mu);
     auto it = g_tune_table.find(key);
     if (it != g_tune_table.end()) return it->second;
+    if (t_no_tuning_runs) return -1;   // a caller that must not block: heuristic tile
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
       return -1;
@@ -534,7 +537,7 @@ int tuned_choice(const ContractDescT<T>& d, const KParams<T>& p, cudaStream_t st
     g_tune_table[key] = best;
     append_record(key, best);
   }
-  tuned = true;   // every candidate overwrote C with the full result
+  tuned = true;
   return best;
 }
 
@@ -558,7 +561,8 @@ void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool determ
   if (!deterministic && autotune_on()) {
     bool tuned = false;
     const int c = tuned_choice(d, p, stream, tuned);
-    if (tuned) return;
+    // after tuning, C holds the last candidate's result: the chosen tile runs once more, so the
+    // first launch of a class gives what every later launch of the class computes
     if (c >= 0) {
       const TileCfg& t = kCandidates[c];
       launch_tiles(d, p, t.bm, t.bn, t.split ? heuristic_split(d, t.bm, t.bn, sms, true) : 1,
@@ -590,6 +594,9 @@ int64_t autotune_classes() {
   std::shared_lock<std::shared_mutex> g(g_tune_mu);
   return (int64_t)g_tune_table.size();
 }
+
+NoTuningScope::NoTuningScope() : prev_(t_no_tuning_runs) { t_no_tuning_runs = true; }
+NoTuningScope::~NoTuningScope() { t_no_tuning_runs = prev_; }
 
 Fp64EngineScope::Fp64EngineScope(int engine) : prev_(t_fp64_engine) { t_fp64_engine = engine; }
 Fp64EngineScope::~Fp64EngineScope() { t_fp64_engine = prev_; }

@@ -56,6 +56,17 @@ struct Fp64EngineScope {
   int prev_;
 };
 
+// Within this scope the calling thread's contractions run no tile-tuning measurements (which
+// synchronise the host): a shape class that already has a record uses it, others the heuristic.
+struct NoTuningScope {
+  NoTuningScope();
+  ~NoTuningScope();
+  NoTuningScope(const NoTuningScope&) = delete;
+  NoTuningScope& operator=(const NoTuningScope&) = delete;
+ private:
+  bool prev_;
+};
+
 // Launches the contraction on `stream`. The tile shape and split-K (C pre-scaled by beta, partial
 // sums added atomically) come from the tile autotuner's record for the launch's shape class, or
 // from an occupancy heuristic (deterministic requests never split K).

@@ -13,6 +13,10 @@
 // start at zero: each call overwrites the parts it reads (the first GEMM writes all of the first
 // intermediate, the second all of the second). Calls that overlap on the GPU (different streams,
 // or different host threads) race on the array and give wrong results; the caller must order them.
+// The product is always the dense contraction (the structured A stage of ttgb_local_product,
+// which applies sparse A cores from their nonzeros, keeps its index tables in allocated memory).
+// The array's device address is looked up once per device and kept for the process: after a
+// cudaDeviceReset the cached address is stale, so this entry point does not support device resets.
 #include <cstdio>
 #include <mutex>
 #include <string>
@@ -67,12 +71,20 @@ extern "C" int ttgb_local_product_noalloc(int64_t rl, int64_t s, int64_t r, int6
     return TTGB_ERR_INVALID;
   }
   const ttgb::LocalOpDims d{rl, s, r, m, n, S, RL, R};
-  const size_t w1 = ttgb::local_product_w1(d), w2 = ttgb::local_product_w2(d);
-  if (w1 + w2 > kNoAllocScratchDoubles) {
+  // scratch sizes rl*s*n*R and rl*m*S*R with overflow checks: a wrapped product could pass the
+  // size test below and let the kernels write past the static array
+  uint64_t w1 = 0, w2 = 0, wsum = 0;
+  const bool wrapped =
+      __builtin_mul_overflow((uint64_t)rl, (uint64_t)s, &w1) || __builtin_mul_overflow(w1, (uint64_t)n, &w1) ||
+      __builtin_mul_overflow(w1, (uint64_t)R, &w1) || __builtin_mul_overflow((uint64_t)rl, (uint64_t)m, &w2) ||
+      __builtin_mul_overflow(w2, (uint64_t)S, &w2) || __builtin_mul_overflow(w2, (uint64_t)R, &w2) ||
+      __builtin_add_overflow(w1, w2, &wsum);
+  if (wrapped || wsum > kNoAllocScratchDoubles) {
     snprintf(msg, sizeof(msg),
-             "ttgb_local_product_noalloc: this product needs %zu doubles of scratch "
+             "ttgb_local_product_noalloc: this product needs %s doubles of scratch "
              "(rl*s*n*R + rl*m*S*R), more than the %zu (32 MiB) the entry point holds; "
-             "use ttgb_local_product", w1 + w2, kNoAllocScratchDoubles);
+             "use ttgb_local_product", wrapped ? "more than 2^64" : std::to_string(wsum).c_str(),
+             kNoAllocScratchDoubles);
     fail(msg);
     return TTGB_ERR_INVALID;
   }
@@ -86,6 +98,8 @@ extern "C" int ttgb_local_product_noalloc(int64_t rl, int64_t s, int64_t r, int6
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   try {
+    // no tile-tuning runs here: they time candidates with events and synchronise the host
+    ttgb::NoTuningScope no_tuning;
     for (int32_t i = 0; i < nrhs; ++i)
       ttgb::local_product(d, phi_l, A, phi_r, x + (int64_t)i * r * n * R,
                           y + (int64_t)i * rl * m * RL, base, base + w1, st);
@@ -93,6 +107,13 @@ extern "C" int ttgb_local_product_noalloc(int64_t rl, int64_t s, int64_t r, int6
     snprintf(msg, sizeof(msg), "ttgb_local_product_noalloc: %s", err.what());
     fail(msg);
     return err.status;
+  } catch (const std::exception& err) {
+    snprintf(msg, sizeof(msg), "ttgb_local_product_noalloc: %s", err.what());
+    fail(msg);
+    return TTGB_ERR_INTERNAL;
+  } catch (...) {
+    fail("ttgb_local_product_noalloc: unknown error");
+    return TTGB_ERR_INTERNAL;
   }
   return TTGB_OK;
 }

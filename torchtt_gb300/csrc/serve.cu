@@ -1,9 +1,11 @@
 // Request server for batched / served AMEn solves (declared in include/ttgb300.h).
 //
 // `slots` host worker threads each own a non-blocking CUDA stream and run one solve at a time,
-// so up to `slots` solves overlap on the GPU. Admission is FIFO and by estimated footprint: the
-// head request starts when a worker is free and its footprint fits in what the running requests
-// leave of the budget (a request larger than the whole budget runs alone).
+// so up to `slots` solves overlap on the GPU. Admission is FIFO and by footprint: the head
+// request starts when a worker is free and its footprint fits in what the running requests leave
+// of the budget (a request larger than the whole budget runs alone). The footprint is an upper
+// bound (footprint_bound: every buffer at the largest rank the solve can reach), so the ranks a
+// running solve grows to never take the budget past what admission reserved.
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -55,23 +57,6 @@ TTView copy_view(const ttgb_tt* t, bool matrix) {
   return v;
 }
 
-// Estimated device bytes of one solve: per core x, z and the four interfaces at the estimated rank,
-// plus the local working set of the largest core (Krylov basis and contraction intermediates).
-size_t estimate_footprint(const TTView& A, const TTView& b, const AmenParams& p) {
-  int64_t nmax = 1, smax = 1, rbmax = 1;
-  for (int k = 0; k < A.d; ++k) {
-    nmax = std::max<int64_t>(nmax, A.cols[k]);
-    smax = std::max<int64_t>(smax, A.ranks[k + 1]);
-    rbmax = std::max<int64_t>(rbmax, b.ranks[k + 1]);
-  }
-  // the solution rank grows to a few times the rhs rank plus the enrichment
-  int64_t r = std::min<int64_t>(p.rmax, 4 * (rbmax + p.kickrank + p.kick2) + 16);
-  const double core = (double)r * r * nmax;
-  const double per_core = 2 * core + 4.0 * r * r * smax;
-  const double local = (p.local_iterations + 1) * core + 2.0 * core * smax + 8 * core;
-  return (size_t)(8.0 * (A.d * per_core + local)) + (64u << 20);
-}
-
 }  // namespace
 
 struct ttgb_server {
@@ -79,6 +64,7 @@ struct ttgb_server {
   int slots = 1;
   size_t budget = 0;
   size_t in_use = 0;
+  size_t peak_in_use = 0;
   int running = 0;
   int peak = 0;
   int64_t next_id = 1;
@@ -108,6 +94,7 @@ struct ttgb_server {
         req = queue.front();
         queue.pop_front();
         in_use += req->footprint;
+        peak_in_use = std::max(peak_in_use, in_use);
         ++running;
         peak = std::max(peak, running);
         req->t_start = Clock::now();
@@ -182,7 +169,7 @@ int ttgb_server_submit(ttgb_server* srv, const ttgb_tt* A, const ttgb_tt* b, con
     TTGB_REQUIRE(req->A.d >= 1 && req->A.d == req->b.d, "Dimension mismatch.");
     req->p = params_from_c(params);
     const AmenParams& p = req->p;
-    req->footprint = estimate_footprint(req->A, req->b, p);
+    req->footprint = footprint_bound(req->A, req->b, req->x0, p);
     std::lock_guard<std::mutex> lock(srv->mu);
     TTGB_REQUIRE(!srv->stopping, "server is shutting down");
     req->id = srv->next_id++;
@@ -239,6 +226,17 @@ int ttgb_server_stats(const ttgb_server* srv, int64_t* submitted, int64_t* compl
   if (completed) *completed = s->completed;
   if (running) *running = s->running;
   if (peak_running) *peak_running = s->peak;
+  return TTGB_OK;
+}
+
+int ttgb_server_memory(const ttgb_server* srv, int64_t* budget, int64_t* in_use,
+                       int64_t* peak_in_use) {
+  if (!srv) return TTGB_ERR_INVALID;
+  auto* s = const_cast<ttgb_server*>(srv);
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (budget) *budget = (int64_t)s->budget;
+  if (in_use) *in_use = (int64_t)s->in_use;
+  if (peak_in_use) *peak_in_use = (int64_t)s->peak_in_use;
   return TTGB_OK;
 }
 

@@ -89,6 +89,13 @@ class Server:
         return {"submitted": sub.value, "completed": comp.value, "running": run.value,
                 "peak_running": peak.value}
 
+    def memory(self):
+        """Admission accounting: ``budget``, ``in_use`` (bytes reserved by running requests) and
+        ``peak_in_use`` (the most reserved at once so far)."""
+        b, u, pk = _lib.c_i64(), _lib.c_i64(), _lib.c_i64()
+        _lib.check(self._L.ttgb_server_memory(self._h, ctypes.byref(b), ctypes.byref(u), ctypes.byref(pk)))
+        return {"budget": b.value, "in_use": u.value, "peak_in_use": pk.value}
+
     def close(self):
         if self._h:
             self._L.ttgb_server_destroy(self._h)
@@ -106,3 +113,29 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def footprint(A, b, x0=None, preconditioner=None, **params):
+    """Upper bound of the device bytes one solve of A x = b allocates (the server's admission unit,
+    ``ttgb_footprint``): every core, interface and workspace at the largest rank the solve can
+    reach, rank(x0) + nswp (kickrank + kick2), capped by rmax and the mode sizes."""
+    keep = []
+    dev = b.cores[0].device if b.cores[0].is_cuda else torch.device("cuda", torch.cuda.current_device())
+    Ac, bc = _prep(A.cores, dev), _prep(b.cores, dev)
+    xc = _prep(x0.cores, dev) if x0 is not None else None
+    dA, db = _desc(Ac, True, keep), _desc(bc, False, keep)
+    dx = _desc(xc, False, keep) if xc else None
+    p = make_params(preconditioner=_PREC[preconditioner], **params)
+    out = _lib.c_i64()
+    _lib.check(_lib.lib().ttgb_footprint(ctypes.byref(dA), ctypes.byref(db),
+                                         ctypes.byref(dx) if dx is not None else None,
+                                         ctypes.byref(p), ctypes.byref(out)))
+    return out.value
+
+
+def pool_usage(reset_high=False):
+    """Bytes the library holds in the device's default memory pool now and at most since the last
+    reset: ``(used_now, used_high)``."""
+    now, high = _lib.c_i64(), _lib.c_i64()
+    _lib.check(_lib.lib().ttgb_pool_usage(ctypes.byref(now), ctypes.byref(high), int(bool(reset_high))))
+    return now.value, high.value

@@ -25,6 +25,20 @@ def _is_tt(x):
     return hasattr(x, "cores") and hasattr(x, "is_ttm")
 
 
+def _rows(x):
+    """Row mode sizes of a TT-matrix (``x.M`` when the class has it, else from the cores)."""
+    M = getattr(x, "M", None)
+    return [int(m) for m in M] if M is not None else [int(c.shape[1]) for c in x.cores]
+
+
+def _cols(x):
+    """Column mode sizes of a TT-matrix, or the mode sizes of a TT-vector (``x.N`` or the cores)."""
+    N = getattr(x, "N", None)
+    if N is not None:
+        return [int(n) for n in N]
+    return [int(c.shape[2] if x.is_ttm else c.shape[1]) for c in x.cores]
+
+
 def _desc(cores, matrix, keep):
     """Build a ttgb_tt descriptor for device tensors; `keep` holds the ctypes arrays alive."""
     d = len(cores)
@@ -158,9 +172,9 @@ def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kick
         raise InvalidArguments('A and b must be TT instances.')
     if not (A.is_ttm and not b.is_ttm):
         raise IncompatibleTypes('A must be TT-matrix and b must be vector.')
-    if list(A.M) != list(A.N):
+    if _rows(A) != _cols(A):
         raise ShapeMismatch('A is not quadratic.')
-    if list(A.N) != list(b.N):
+    if _cols(A) != _cols(b):
         raise ShapeMismatch('Dimension mismatch.')
     if preconditioner not in _PREC:
         raise InvalidArguments("Invalid preconditioner.")
