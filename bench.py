@@ -266,6 +266,81 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_configs(args, dev, engine, strict):
+    """The batched and served workloads beside the headline, each on a stated sample of its full
+    definition, mixed and plain FP64 through the same server with the same slots (so their ratio
+    is the same-batching mixed/FP64 speed-up), within a wall budget (``--configs-budget-s``) split
+    between them:
+
+    * parametric diffusion (256 systems A(theta) = sum_k theta_k L_k, d=10, n=32, rhs rank U{1..16},
+      eps 1e-8, nswp 40, kickrank 8): every 8th system (32, rhs ranks across 1-16);
+    * rounding stress (128 solves, d=16, n=32, A = L + C C^T + I, b = a sum of 4 random TTs rounded
+      to 1e-8 before the solve): terms of rank 4 (b of rank 16, nswp 40) - with the full terms of
+      rank 16 the reference's own solve does not converge in 20 sweeps (relres 0.70, ranks <= 161);
+    * serving trace (10,000 requests, Poisson arrivals, d U{8..24}, n in {16,32,64}, rhs rank
+      U{1..32}, eps in {1e-6,1e-8,1e-10}): the first 12 requests of the seeded trace at 2
+      requests/s (above capacity, so the replay measures served throughput with queueing)."""
+    import torch
+    from torchtt_gb300 import TT, workloads as W
+    from torchtt_gb300.serving import Server
+    from torchtt_gb300.trace import replay
+
+    t_start = time.perf_counter()
+
+    def served(systems, precision):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        with Server(slots=args.slots, device=dev) as srv:
+            ids = [srv.submit(A, b, precision=precision, engine=engine, seed=7 + i,
+                              strict_eps=strict, **p) for i, (A, b, p) in enumerate(systems)]
+            res = [srv.result(r) for r in ids]
+        el = time.perf_counter() - t0
+        lat = [st["queue_ms"] + st["run_ms"] for _, st in res]
+        rr = [float((A @ x - b).norm() / b.norm()) / p["eps"] for (A, b, p), (x, _) in zip(systems, res)]
+        return {"solves": len(systems), "solves_per_s": len(systems) / el, "elapsed_s": el,
+                "latency_ms": {"p50": percentile(lat, 0.5), "p99": percentile(lat, 0.99)},
+                "max_relres_over_eps": max(rr), "relres_pass_frac": sum(1 for v in rr if v <= 1.0) / len(rr),
+                "max_rank": max(max(st["ranks"]) for _, st in res)}
+
+    def pair(systems, full_count, note):
+        out = {"sample": note, "full_size": full_count}
+        out["mixed"] = served(systems, "mixed")
+        out["fp64"] = served(systems, "fp64")
+        out["mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+        out["extrapolated_full_s"] = {"mixed": full_count / out["mixed"]["solves_per_s"],
+                                      "fp64": full_count / out["fp64"]["solves_per_s"]}
+        return out
+
+    res = {"budget_s": args.configs_budget_s, "server_slots": args.slots, "strict_eps": strict}
+    sysd = [W.parametric_diffusion_d10_n32(i) for i in range(0, 256, 8)]
+    systems = [(TT([c.to(dev) for c in w["A"]]), TT([c.to(dev) for c in w["b"]]), w["params"]) for w in sysd]
+    res["parametric_diffusion_d10_n32"] = pair(
+        systems, 256, "systems 0, 8, .., 248 of the 256 (rhs ranks across 1-16)")
+    if time.perf_counter() - t_start < 0.45 * args.configs_budget_s:
+        systems = []
+        for i in range(8):
+            w = W.rounding_stress(i, term_rank=4, nswp=40)
+            A = TT([c.to(dev) for c in w["A"]])
+            b = TT([c.to(dev) for c in w["b"]]).round(w["round_b"])   # rounded before the clock
+            systems.append((A, b, w["params"]))
+        res["rounding_stress_d16_n32"] = pair(
+            systems, 128, "solves 0-7 of 128 with b = 4 rank-4 terms (rank 16) rounded to 1e-8 on "
+                          "the GPU before the timed region, nswp 40")
+    if time.perf_counter() - t_start < 0.7 * args.configs_budget_s:
+        out = {"sample": "the first 12 requests of the seeded trace (seed 5) at 2 requests/s",
+               "full_size": 10000}
+        out["mixed"] = replay(12, 2.0, slots=args.slots, precision="mixed", engine=engine,
+                              device=dev.index, strict_eps=strict)
+        out["fp64"] = replay(12, 2.0, slots=args.slots, precision="fp64", engine=engine,
+                             device=dev.index, strict_eps=strict)
+        out["mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+        out["extrapolated_full_s"] = {"mixed": 10000 / out["mixed"]["solves_per_s"],
+                                      "fp64": 10000 / out["fp64"]["solves_per_s"]}
+        res["serving_trace"] = out
+    res["elapsed_s"] = time.perf_counter() - t_start
+    return res
+
+
 def read_profile_value(name, key):
     """A ``key: value`` line of a committed ncu summary (per-launch DRAM traffic)."""
     try:
@@ -308,14 +383,16 @@ def run_gb300(args):
 
     srv = Server(slots=args.slots, device=dev)
 
+    strict = args.strict_eps
+
     def batch(precision, A=A_d, rhs=bs_d):
-        ids = [srv.submit(A, b, precision=precision, engine=engine, seed=1000 + j, **kw)
-               for j, b in enumerate(rhs)]
+        ids = [srv.submit(A, b, precision=precision, engine=engine, seed=1000 + j,
+                          strict_eps=strict, **kw) for j, b in enumerate(rhs)]
         return [srv.result(i) for i in ids]
 
     def single(precision, j=0, profile=False):
         return solve_cores(A_d.cores, bs_d[j].cores, precision=precision, engine=engine,
-                           seed=1000 + j, profile=profile, stream=stream, **kw)
+                           seed=1000 + j, profile=profile, stream=stream, strict_eps=strict, **kw)
 
     # ---- headline: mixed precision, batched through the server --------------------------------
     # one untimed solve of each path alone first: the contraction engine's tile autotuner times its
@@ -384,6 +461,7 @@ def run_gb300(args):
 
     res_mixed = [relres(x, b) for (x, _), b in zip(results, bs_d)]
     res_fp64 = relres(x_fp64, bs_d[0])
+    res_fp64_batch = [relres(x, b) for (x, _), b in zip(fp64_batch, bs_d)]
     x_m0 = results[0][0]
     dx = float((x_m0 - x_fp64).norm() / x_fp64.norm())
 
@@ -476,13 +554,31 @@ def run_gb300(args):
     srv_stats = srv.stats()
     srv.close()
 
+    configs = run_configs(args, dev, engine, strict) if (rank == 0 and args.configs_budget_s > 0) else None
+
+    # the cost of guaranteeing relres <= eps: one batched step with strict_eps (AMEn at eps / 4)
+    strict_line = None
+    if rank == 0 and not strict:
+        with Server(slots=args.slots, device=dev) as srv2:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ids = [srv2.submit(A_d, b, precision="mixed", engine=engine, seed=1000 + j,
+                               strict_eps=True, **kw) for j, b in enumerate(bs_d)]
+            out = [srv2.result(i) for i in ids]
+            el = time.perf_counter() - t0
+        rr = [relres(x, b) for (x, _), b in zip(out, bs_d)]
+        strict_line = {"value": nb / el, "unit": "solves/s", "relres_max": max(rr),
+                       "relres_pass_frac": sum(1 for v in rr if v <= p["eps"]) / len(rr),
+                       "how": "one batched step of the same 16 solves with strict_eps (AMEn run at "
+                              "eps / 4 so that the true relres ends <= eps), wall clock"}
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        dt, info = cpu_solve_once(wls[0])
-        cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": "1 full solve of %s (b seed %d) with the numpy restatement of the reference "
-                         "(oracle/amen.py), numpy/OpenBLAS threads = all host cores"
-                         % (args.workload, seeds[0])}
+        solve_ref, kind, how = reference_solver()
+        dt = solve_ref(wls[0])
+        cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": os.cpu_count() or 1, "kind": kind,
+               "sample": "1 full solve of %s (b seed %d): %s, threads = all host cores"
+                         % (args.workload, seeds[0], how)}
 
     if rank == 0:
         cfg = arm_config(args, wls[0], ws)
@@ -496,12 +592,18 @@ def run_gb300(args):
             "fp64_plain": {"value": fp64_value, "unit": "solves/s", "ms_per_solve": statistics.mean(fp64_ms),
                            "solves": len(fp64_ms), "relres": res_fp64},
             "speedup_vs_fp64_plain": value / fp64_value,
+            "speedup_vs_fp64_batched": value / (1000.0 * nb / fp64_batch_ms),
             "mixed_single": {"ms_per_solve": mixed_single_ms, "value": 1000.0 / mixed_single_ms,
                              "refinements": mixed_stats["refinements"],
                              "lowp_matvecs": mixed_stats["lowp_matvecs"], "matvecs": mixed_stats["matvecs"]},
             "fp64_batched": {"value": 1000.0 * nb / fp64_batch_ms, "unit": "solves/s", "ms_per_step": fp64_batch_ms},
             "accuracy": {"relres_max": max(res_mixed), "relres_fp64": res_fp64,
-                         "x_mixed_vs_fp64": dx, "eps": p["eps"]},
+                         "relres_fp64_batched_max": max(res_fp64_batch),
+                         "relres_pass_frac": sum(1 for v in res_mixed if v <= p["eps"]) / len(res_mixed),
+                         "relres_pass_frac_fp64": sum(1 for v in res_fp64_batch if v <= p["eps"]) / len(res_fp64_batch),
+                         "x_mixed_vs_fp64": dx, "eps": p["eps"],
+                         "stopping": "strict_eps (AMEn at eps/4)" if strict
+                                     else "the reference's rule (max local residual < eps)"},
             "solve": {"sweeps": mixed_stats["sweeps"], "max_rank": max(mixed_stats["ranks"]),
                       "gmres_iterations": mixed_stats["gmres_iterations"],
                       "host_syncs": mixed_stats["host_syncs"]},
@@ -515,6 +617,8 @@ def run_gb300(args):
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "gpu_launches": int(launches),
             "clocks": clocks,
+            "configs": configs,
+            "strict_eps_mixed": strict_line,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -535,6 +639,11 @@ def main():
     ap.add_argument("--fp64-solves", type=int, default=2)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--configs-budget-s", type=float, default=150.0,
+                    help="wall budget of the batched/served workloads block (0: skip it)")
+    ap.add_argument("--strict-eps", action="store_true",
+                    help="solve every system to a true relres <= eps (strict_eps: AMEn at eps / 4); "
+                         "default: the reference's stopping rule, with the pass fraction reported")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

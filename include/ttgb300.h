@@ -73,7 +73,15 @@ typedef struct ttgb_amen_params {
                                    path when eps >= 1e-9 and A and b fit the FP32 exponent range,
                                    ~1e-13 relative; native FP64 otherwise), 1 native FP64,
                                    2 double-float.
-                                   QR and SVD always run in native FP64. */
+                                   On the MIXED path with double-float products the GEMMs
+                                   of the QR/SVD (CholeskyQR Gram and apply products) run in
+                                   double-float too; the factorisations themselves (Cholesky,
+                                   Jacobi rotations) always run in native FP64. */
+  int32_t strict_eps;           /* 0 (default): the reference's tolerance and stopping rule,
+                                   which bound the local residuals (its true residual can end a
+                                   few times above eps); 1: the sweeps solve, truncate and stop
+                                   at eps / 4, so that the true relative residual ends at or
+                                   below eps (at the cost of higher ranks and more sweeps) */
 } ttgb_amen_params;
 
 /* Precision modes. FP64: the reference's arithmetic. MIXED: the local GMRES applies the projected

@@ -161,3 +161,23 @@ def test_double_float_products_match_native(cuda, fixture):
     assert float((TT(xd) - TT(xn)).norm() / TT(xn).norm()) <= 10 * p["eps"]
     _parity.check(A, b, [c.cpu().numpy() for c in xd], G.cores(z, "x_cpp"), p["eps"],
                   p["kickrank"], label="double-float " + fixture)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_strict_eps_reaches_eps(cuda, precision):
+    """strict_eps (AMEn at eps / 4) takes the true relative residual of the d=20 n=64 benchmark
+    solve to eps, where the reference's own rule on the same input ends at 3.4e-8; the solution
+    stays within 10 eps of the reference's (sampled estimate) with ranks >= the reference's."""
+    from torchtt_gb300 import TT, amen_solve
+    z = G.load("solve_laplace_potential_d20_n64.npz")
+    A, b, z0 = G.cores(z, "A"), G.cores(z, "b"), G.cores(z, "z0")
+    p = G.params(z)
+    x = amen_solve(TT(to_dev(A, cuda)), TT(to_dev(b, cuda)), nswp=p["nswp"], eps=p["eps"],
+                   kickrank=p["kickrank"], z0=to_dev(z0, cuda), precision=precision, strict_eps=True)
+    xs = [c.cpu().numpy() for c in x.cores]
+    from oracle import amen as O
+    res = O.tt_relres(A, xs, b)
+    err = _parity.sampled_relerr(xs, z)
+    assert res <= p["eps"], (precision, res)
+    assert err <= 10 * p["eps"], (precision, err)
+    assert all(r >= rr for r, rr in zip([c.shape[0] for c in xs], z["ref_ranks"][:-1]))

@@ -29,6 +29,23 @@ def test_lowp_local_product(cuda, engine, shape):
     assert np.abs(y - ref).max() <= 1e-4 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("rR", [(60, 60), (5, 7), (81, 77), (1, 9)])
+def test_tc_local_product_structured_core(cuda, rR):
+    """The tcgen05 engine with a sparse Kronecker-sum core (structured A stage between the two
+    tensor-core GEMMs, its output written as the padded TF32 split the second GEMM's TMA reads),
+    against the FP64 oracle at the engine's 1e-5."""
+    from torchtt_gb300 import ops, workloads as W
+    r, R = rR
+    A = W.laplace_potential_ttm(4, 64)[1].numpy()       # 3 x 64 x 64 x 3
+    s, n, S = A.shape[0], A.shape[1], A.shape[3]
+    g = np.random.default_rng(r * 1000 + R)
+    PhiL, PhiR, x = g.standard_normal((r, s, r)), g.standard_normal((R, S, R)), g.standard_normal((r, n, R))
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    y = ops.local_product_lowp(t(PhiR), t(PhiL), t(A), t(x), engine=2).cpu().numpy()
+    ref = O.local_product(PhiR, PhiL, A, x)
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-5
+
+
 @pytest.mark.parametrize("shape", [(60, 3, 64, 3, 60), (1, 3, 64, 3, 9), (171, 2, 32, 2, 20),
                                    (5, 2, 12, 2, 7)])
 def test_double_float_local_product(cuda, shape):

@@ -31,7 +31,7 @@ class AmenParams(ctypes.Structure):
                 ("kickrank", c_i32), ("kick2", c_i32), ("local_iterations", c_i32),
                 ("resets", c_i32), ("verbose", c_i32), ("preconditioner", c_i32), ("seed", c_u64),
                 ("profile", c_i32), ("precision", c_i32), ("lowp_engine", c_i32),
-                ("a_structure", c_i32), ("fp64_engine", c_i32)]
+                ("a_structure", c_i32), ("fp64_engine", c_i32), ("strict_eps", c_i32)]
 
 PRECISION = {"fp64": 0, "mixed": 1}
 

@@ -3,6 +3,8 @@
 // the norm bookkeeping scalars (normA/normb/normx/nrmsc, amen_solve.h:195-204) and the stopping
 // decisions; it reads device scalars in small batches (one synchronisation per group of norms).
 #include <algorithm>
+#include <cstdlib>
+#include <string>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -153,6 +155,9 @@ class AmenRun {
   int64_t op_count_ = 0;   // applications of the current local operator
   int64_t lowp_count_ = 0; // low-precision applications of the current local operator
   bool mixed_ = false;
+  // tolerance of the sweeps: eps, or eps / 4 with strict_eps (the reference's stopping rule bounds
+  // the local residuals; its true residual can end a few times above them)
+  double eps_ = 0.0;
   int fp64e_ = kFp64Native;   // engine of the FP64 products (double-float on the mixed path)
   std::vector<FBuf> A32_;  // FP32 copies of the A cores (mixed path, FP32 engine)
   FBuf phil32_, phir32_, xf_, yf_, w1f_, w2f_;
@@ -290,6 +295,7 @@ void AmenRun::init(const TTView& x0, const TTView& z0) {
   if (p_.a_structure)
     for (int i = 0; i < d; ++i) spA_[i].build(Acore(i), rA_[i], N_[i], N_[i], rA_[i + 1], s_);
   mixed_ = p_.precision == 1;
+  eps_ = p_.strict_eps ? 0.25 * p_.eps : p_.eps;
   fp64e_ = choose_fp64_engine();
   if (mixed_) {
     use_tc_ = (p_.lowp_engine == 2) || (p_.lowp_engine == 0 && tc_available());
@@ -493,7 +499,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
   const int64_t rk = rx_[k], rk1 = rx_[k + 1];
   const int64_t nl = rk * n * rk1;
   const double damp = 2.0;
-  const double real_tol = (p_.eps / std::sqrt((double)d_)) / damp;   // amen_solve.h:309
+  const double real_tol = (eps_ / std::sqrt((double)d_)) / damp;   // amen_solve.h:309
 
   phase(kPhFwdSetup);
   DBuf rhs((size_t)nl, s_), sol((size_t)nl, s_), tmp((size_t)nl, s_);
@@ -873,8 +879,28 @@ void AmenRun::z_update_forward(int k, const double* trunc) {
   z_[k] = std::move(zk);
 }
 
+// Engine of the GEMMs of the mixed path's dense linear algebra (the CholeskyQR3 Gram and apply
+// products, U = Q V', the enrichment's block Gram-Schmidt, reconstructions): double-float whenever
+// the mixed path's FP64 products are double-float. Those GEMMs dominate the SM time of a solve on
+// GB300's FP64 pipe; in double-float they keep ~1e-13 of the sum of magnitudes of their terms,
+// Q stays orthogonal to ~1e-13 (CholeskyQR3's third pass), far below the eps >= 1e-9 where the
+// double-float engine is chosen. The Cholesky factorisations, the Jacobi rotations, Gram-Schmidt
+// of the Krylov basis and every norm stay native FP64. TTGB_LA_ENGINE=native keeps them native.
+static int linalg_engine(int fp64_products_engine, double eps) {
+  static const bool force_native = [] {
+    const char* e = std::getenv("TTGB_LA_ENGINE");
+    return e != nullptr && std::string(e) == "native";
+  }();
+  // only where the automatic choice takes double-float at all (eps >= 1e-9): a caller that forces
+  // double-float products below that keeps the factorisations' GEMMs native
+  return (fp64_products_engine == kFp64DoubleFloat && eps >= 1e-9 && !force_native)
+             ? kFp64DoubleFloat : kFp64Native;
+}
+
 AmenResult AmenRun::run(const TTView& x0, const TTView& z0) {
   init(x0, z0);
+  // every contraction issued by this solve's thread outside the scopes of the FP64 products
+  Fp64EngineScope la_engine(mixed_ ? linalg_engine(fp64e_, p_.eps) : kFp64Native);
   bool last = false;
   int swp = 0;
   double max_res = 0.0;
@@ -890,7 +916,7 @@ AmenResult AmenRun::run(const TTView& x0, const TTView& z0) {
       std::printf(" ] max_res %g elapsed %.3f s\n", max_res, el);
     }
     if (last) break;   // amen_solve.h:522-526
-    if (max_res < p_.eps) last = true;
+    if (max_res < eps_) last = true;
   }
   phase(kPhOther);
   st_.sweeps = swp < p_.nswp ? swp + 1 : swp;

@@ -33,6 +33,9 @@ struct AmenParams {
   // (double-float on the mixed path when A and b lie within the FP32 exponent range, native FP64
   // otherwise), 1 native FP64, 2 double-float. QR/SVD always run in native FP64.
   int fp64_engine = 0;
+  // 1: the sweeps solve, truncate and stop at eps / 4, so that the true relative residual ends at
+  // or below eps (the reference's rule bounds only the local residuals)
+  int strict_eps = 0;
 };
 
 // A TT-matrix or TT-vector given by device pointers (borrowed).

@@ -132,6 +132,8 @@ AmenParams params_from_c(const ttgb_amen_params* params) {
   p.a_structure = params->a_structure;
   TTGB_REQUIRE(params->fp64_engine >= 0 && params->fp64_engine <= 2, "invalid fp64_engine");
   p.fp64_engine = params->fp64_engine;
+  TTGB_REQUIRE(params->strict_eps == 0 || params->strict_eps == 1, "invalid strict_eps");
+  p.strict_eps = params->strict_eps;
   return p;
 }
 }  // namespace ttgb
@@ -156,6 +158,7 @@ void ttgb_default_params(ttgb_amen_params* p) {
   p->lowp_engine = 0;
   p->a_structure = 1;
   p->fp64_engine = 0;
+  p->strict_eps = 0;
 }
 
 int ttgb_amen_solve(const ttgb_tt* A, const ttgb_tt* b, const ttgb_tt* x0, const ttgb_tt* z0,
@@ -550,6 +553,6 @@ int ttgb_pool_usage(int64_t* used_now, int64_t* used_high, int32_t reset_high) {
   });
 }
 
-int32_t ttgb_version(void) { return 101; }
+int32_t ttgb_version(void) { return 102; }
 
 }  // extern "C"

@@ -17,6 +17,7 @@ namespace ttgb {
 // A' [(m,S),(s,n)] split of one A core (s x m x n x S), shared by every local problem of that core
 struct TcCore {
   FBuf hi, lo;
+  int64_t ld = 0;   // row pitch of A' (s n rounded up to 4 floats)
   void build(const double* A, int64_t s, int64_t m, int64_t n, int64_t S, cudaStream_t st);
 };
 
@@ -25,6 +26,7 @@ struct TcLocal {
   const TcCore* core = nullptr;
   const SparseCore* sp = nullptr;   // when sp->use, the A stage runs from the nonzeros (FP32)
   FBuf phl_h, phl_l, phr_h, phr_l, xh, xl, wh, wl, yh, yl, wf;
+  int64_t ld_r = 0, ld_sn = 0, ld_SR = 0;   // padded row pitches of the K-major operands
   int* err = nullptr;   // device flag of the bounded waits
   void setup(const LocalOpDims& dims, const double* phi_l, const double* phi_r, const TcCore* c,
              const SparseCore* spa, int* errflag, cudaStream_t st);

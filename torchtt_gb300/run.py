@@ -36,7 +36,12 @@ def main():
                     help="skip the relative residual (runs no kernel after the solve)")
     ap.add_argument("--served", type=int, default=0,
                     help="submit all solves at once to a server with this many slots")
+    ap.add_argument("--local-product", default=None, metavar="R,S,N,S2,R2",
+                    help="run only the low-precision local product (tcgen05 engine) of this shape "
+                         "(r, s, n, S, R) with a Laplacian-plus-potential core, --solves times")
     args = ap.parse_args()
+    if args.local_product:
+        return local_product(args)
     if args.served > 0:
         return served(args)
     if args.workload == "laplace_d8_n16":
@@ -65,6 +70,34 @@ def main():
                           "ranks": st["ranks"], "matvecs": st["matvecs"],
                           "lowp_matvecs": st["lowp_matvecs"], "refinements": st["refinements"],
                           "gmres_iterations": st["gmres_iterations"]}), flush=True)
+
+
+def local_product(args):
+    """The mixed path's low-precision local product alone (a profiler target for its kernels):
+    Phi_left, Phi_right and x random, the A core of the d=20 n=64 workload's operator (a middle
+    core of the Laplacian plus potential, applied from its nonzeros) when n = 64 and S = 3, a
+    random dense core otherwise."""
+    import numpy as np
+    import torch
+
+    from . import ops, workloads as W
+
+    r, s, n, S, R = (int(v) for v in args.local_product.split(","))
+    dev = torch.device("cuda", 0)
+    g = np.random.default_rng(args.seed)
+    A = (W.laplace_potential_ttm(4, n)[1].numpy() if (s, S) == (3, 3)
+         else g.standard_normal((s, n, n, S)))
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    PhiL, PhiR, x = t(g.standard_normal((r, s, r))), t(g.standard_normal((R, S, R))), t(g.standard_normal((r, n, R)))
+    Ad = t(A)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.solves):
+        y = ops.local_product_lowp(PhiR, PhiL, Ad, x, engine=2)
+    torch.cuda.synchronize()
+    print(json.dumps({"local_product": [r, s, n, S, R], "repeats": args.solves,
+                      "ms_per_product": 1000 * (time.perf_counter() - t0) / args.solves,
+                      "norm": float(y.norm())}), flush=True)
 
 
 def served(args):

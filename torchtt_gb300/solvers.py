@@ -65,7 +65,7 @@ def _prep(cores, device):
 def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-10, rmax=32768,
                 max_full=500, kickrank=4, kick2=0, local_iterations=40, resets=2, verbose=False,
                 preconditioner=0, seed=1, stream=None, precision="fp64", profile=False,
-                engine="auto", a_structure=True, fp64_engine="auto"):
+                engine="auto", a_structure=True, fp64_engine="auto", strict_eps=False):
     """Native solve on lists of CUDA float64 cores; returns ``(x_cores, stats_dict)``.
 
     This is the thin layer over ``ttgb_amen_solve`` (include/ttgb300.h); ``amen_solve`` below adds
@@ -80,7 +80,8 @@ def solve_cores(A_cores, b_cores, x0_cores=None, z0_cores=None, nswp=22, eps=1e-
     p = make_params(nswp=nswp, eps=eps, rmax=rmax, max_full=max_full, kickrank=kickrank,
                     kick2=kick2, local_iterations=local_iterations, resets=resets, verbose=verbose,
                     preconditioner=preconditioner, seed=seed, precision=precision, profile=profile,
-                    engine=engine, a_structure=a_structure, fp64_engine=fp64_engine)
+                    engine=engine, a_structure=a_structure, fp64_engine=fp64_engine,
+                    strict_eps=strict_eps)
     if stream is None:
         stream = torch.cuda.current_stream(A_cores[0].device)
     handle = _lib.c_vp()
@@ -120,10 +121,12 @@ def fetch_solution(handle, modes, device, stream):
 def make_params(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=0,
                 local_iterations=40, resets=2, verbose=False, preconditioner=0, seed=1,
                 precision="fp64", profile=False, engine="auto", a_structure=True,
-                fp64_engine="auto"):
+                fp64_engine="auto", strict_eps=False):
     """A ``ttgb_amen_params`` structure from keyword arguments (defaults of the reference).
     ``a_structure=False`` forces the dense contraction of the A cores; ``fp64_engine`` is
-    'auto' (double-float FP64 products on the mixed path), 'native' or 'df'."""
+    'auto' (double-float FP64 products on the mixed path), 'native' or 'df'; ``strict_eps``
+    runs the sweeps at eps / 4 so that the true residual ends at or below eps (the reference's
+    rule bounds the local residuals only, and its true residual can end a few times above eps)."""
     p = _lib.AmenParams()
     _lib.lib().ttgb_default_params(ctypes.byref(p))
     p.nswp, p.eps, p.rmax, p.max_full = int(nswp), float(eps), int(rmax), int(max_full)
@@ -143,6 +146,7 @@ def make_params(nswp=22, eps=1e-10, rmax=32768, max_full=500, kickrank=4, kick2=
     if fp64_engine not in engines64:
         raise InvalidArguments("fp64_engine must be 'auto', 'native' or 'df'")
     p.fp64_engine = engines64[fp64_engine]
+    p.strict_eps = int(bool(strict_eps))
     return p
 
 
@@ -150,7 +154,7 @@ def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kick
                trunc_norm='res', local_solver=1, local_iterations=40, resets=2, verbose=False,
                preconditioner=None, use_cpp=True, band_diagonal=-1, use_single_precision=False,
                backend='gb300', seed=1, z0=None, return_stats=False, precision=None,
-               engine='auto'):
+               engine='auto', strict_eps=False):
     """Solve the multilinear system A x = b in the TT format with AMEn on the GPU.
 
     Arguments are those of ``torchtt.solvers.amen_solve`` (``torchtt/solvers.py:211``), with the same
@@ -165,7 +169,10 @@ def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kick
       GMRES operator inside FP64 iterative refinement). ``use_single_precision=True``, the
       reference's own mixed mode (``torchtt/solvers.py:469-496``), selects ``'mixed'``;
     * ``engine``: low-precision contraction engine of the mixed path, ``'auto'`` (tcgen05 when
-      available), ``'tc'`` (tcgen05 3xTF32 tensor cores) or ``'fp32'`` (FP32 CUDA cores).
+      available), ``'tc'`` (tcgen05 3xTF32 tensor cores) or ``'fp32'`` (FP32 CUDA cores);
+    * ``strict_eps``: the sweeps solve, truncate and stop at eps / 4, so that the true relative
+      residual ends at or below eps (the reference's tolerance, the default, bounds only the local
+      residuals, and its true residual can end a few times above eps).
     """
     # argument checks of torchtt/solvers.py:259-266
     if not (_is_tt(A) and _is_tt(b)):
@@ -192,7 +199,7 @@ def amen_solve(A, b, nswp=22, x0=None, eps=1e-10, rmax=32768, max_full=500, kick
     cores, stats = solve_cores(Ac, bc, xc, zc, nswp=nswp, eps=eps, rmax=rmax, max_full=max_full,
                                kickrank=kickrank, kick2=kick2, local_iterations=local_iterations,
                                resets=resets, verbose=verbose, preconditioner=_PREC[preconditioner],
-                               seed=seed, engine=engine,
+                               seed=seed, engine=engine, strict_eps=strict_eps,
                                precision=precision or ("mixed" if use_single_precision else "fp64"))
     cores = [c.to(device=out_device, dtype=out_dtype) for c in cores]
     cls = type(b) if _is_tt(b) else TT

@@ -29,7 +29,7 @@ def _percentile(xs, q):
 
 
 def replay(count, rate, slots=8, precision="mixed", engine="auto", seed=5, mem_budget_bytes=0,
-           check=True, device=None, max_d=24, ranks=(1, 32), modes=(16, 32, 64)):
+           check=True, device=None, max_d=24, ranks=(1, 32), modes=(16, 32, 64), strict_eps=False):
     """Replays ``count`` requests arriving at ``rate`` per second; ``max_d``, ``ranks`` and
     ``modes`` bound the request sizes (full size: 24, (1, 32), (16, 32, 64))."""
     dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
@@ -49,7 +49,7 @@ def replay(count, rate, slots=8, precision="mixed", engine="auto", seed=5, mem_b
             if wait > 0:
                 time.sleep(wait)
             ids.append(srv.submit(A, b, precision=precision, engine=engine, seed=1000 + i,
-                                  **w["params"]))
+                                  strict_eps=strict_eps, **w["params"]))
         results = [srv.result(r) for r in ids]
         elapsed = time.perf_counter() - t0
         peak = srv.stats()["peak_running"]
@@ -66,6 +66,9 @@ def replay(count, rate, slots=8, precision="mixed", engine="auto", seed=5, mem_b
             rr = float((A @ x - b).norm() / b.norm())
             worst = max(worst, rr / w["params"]["eps"])
         out["max_relres_over_eps"] = worst
+        out["relres_pass_frac"] = sum(
+            1 for (x, _), (_, _, w, A, b) in zip(results, reqs)
+            if float((A @ x - b).norm() / b.norm()) <= w["params"]["eps"]) / count
         out["unconverged"] = sum(1 for _, st in results if not st.get("converged", 1))
     return out
 
