@@ -1,9 +1,10 @@
 """Solve-level parity criteria against the reference's solution on the same inputs.
 
-* relative residual ||A x - b|| / ||b|| <= max(10 eps, 2 x the reference's own on the same input):
-  the reference stops on its local residual (cpp/amen_solve.h:375,525), so its true residual can
-  exceed eps; on the random 4x5x6 system of tests/test_solvers.py it ranges from 2e-11 to 7e-10 at
-  eps = 1e-10 depending on the random enrichment start alone;
+* relative residual ||A x - b|| / ||b|| <= eps where the reference reaches eps on the same input,
+  else <= 2 x the reference's own: the reference stops on its local residual
+  (cpp/amen_solve.h:375,525), so its true residual can exceed eps (3.4e-8 at eps 1e-8 on the d=20
+  n=64 benchmark solve; from 2e-11 to 7e-10 at eps 1e-10 on the random 4x5x6 system of
+  tests/test_solvers.py, depending on the random enrichment start alone);
 * ||x - x_ref|| / ||x_ref|| <= max(10 eps, cond(A) (res + res_ref)) where cond(A) is known (small
   dense cases), else <= 10 eps;
 * TT ranks within +-kickrank of the reference's.
@@ -13,7 +14,9 @@ import numpy as np
 from oracle import amen as O
 
 
-def check(A, b, x, x_ref, eps, kickrank, cond=None, label=""):
+def check(A, b, x, x_ref, eps, kickrank, cond=None, label="", res_slack=1.0):
+    """``res_slack`` > 1 widens the residual bar (the numpy restatement's trajectory differs from
+    ATen's in rounding, and AMEn's stopping rule bounds the true residual only up to a factor)."""
     A = [np.asarray(a) for a in A]
     b = [np.asarray(c) for c in b]
     x = [np.asarray(c) for c in x]
@@ -24,9 +27,10 @@ def check(A, b, x, x_ref, eps, kickrank, cond=None, label=""):
     bound = 10 * eps if cond is None else max(10 * eps, cond * (res + res_ref))
     ranks = [c.shape[2] for c in x][:-1]
     ranks_ref = [c.shape[2] for c in x_ref][:-1]
-    msg = "%s res %.3e (ref %.3e) err %.3e (bound %.3e) ranks %s ref %s" % (
-        label, res, res_ref, err, bound, ranks, ranks_ref)
-    assert res <= max(10 * eps, 2 * res_ref), msg
+    msg = "%s res %.3e (ref %.3e, bar %.3e) err %.3e (bound %.3e) ranks %s ref %s" % (
+        label, res, res_ref, res_slack * res_bound(eps, res_ref), err, bound, ranks, ranks_ref)
+    print(msg)
+    assert res <= res_slack * res_bound(eps, res_ref), msg
     assert err <= bound, msg
     assert all(abs(a - c) <= kickrank for a, c in zip(ranks, ranks_ref)), msg
     return res, res_ref, err
