@@ -266,11 +266,52 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def tt_relres_check(A_cores, x_cores, b_cores):
+    """||A x - b|| / ||b|| of TT cores on the GPU, for the accuracy fields of the JSON line (a
+    check on the solutions, outside every timed region): the residual's cores [A_k x_k, -b_k]
+    (ranks add) are orthogonalised right to left with Householder QR (torch.linalg.qr), which keeps
+    the accuracy of a norm ~1e-8 of its parts' norms."""
+    import torch
+    d = len(A_cores)
+
+    def core(k):
+        a, x, b = A_cores[k], x_cores[k], b_cores[k]
+        s, m, _, S = a.shape
+        r, _, R = x.shape
+        y = torch.einsum("smnS,rnR->srmSR", a, x).reshape(s * r, m, S * R)
+        if d == 1:
+            return y - b
+        if k == 0:
+            return torch.cat([y, -b], dim=2)
+        if k == d - 1:
+            return torch.cat([y, b], dim=0)
+        out = torch.zeros((y.shape[0] + b.shape[0], m, y.shape[2] + b.shape[2]),
+                          dtype=y.dtype, device=y.device)
+        out[:y.shape[0], :, :y.shape[2]] = y
+        out[y.shape[0]:, :, y.shape[2]:] = b
+        return out
+
+    def norm(cores):
+        cur = None
+        for k in range(len(cores) - 1, -1, -1):
+            c = cores[k]
+            if cur is not None:
+                c = torch.tensordot(c, cur, dims=([2], [0]))
+            if k == 0:
+                return float(torch.linalg.norm(c))
+            r = c.shape[0]
+            rf = torch.linalg.qr(c.reshape(r, -1).T, mode="r")[1]   # (min, r)
+            cur = rf.T                                               # r x min
+        return 0.0
+
+    return norm([core(k) for k in range(d)]) / norm(list(b_cores))
+
+
 def run_configs(args, dev, engine, strict):
     """The batched and served workloads beside the headline, each on a stated sample of its full
     definition, mixed and plain FP64 through the same server with the same slots (so their ratio
-    is the same-batching mixed/FP64 speed-up), within a wall budget (``--configs-budget-s``) split
-    between them:
+    is the same-batching mixed/FP64 speed-up), within a wall budget (``--configs-budget-s``; a
+    stage's FP64 half runs only when the budget left covers ~2.5x its mixed half):
 
     * parametric diffusion (256 systems A(theta) = sum_k theta_k L_k, d=10, n=32, rhs rank U{1..16},
       eps 1e-8, nswp 40, kickrank 8): every 8th system (32, rhs ranks across 1-16);
@@ -278,37 +319,52 @@ def run_configs(args, dev, engine, strict):
       to 1e-8 before the solve): terms of rank 4 (b of rank 16, nswp 40) - with the full terms of
       rank 16 the reference's own solve does not converge in 20 sweeps (relres 0.70, ranks <= 161);
     * serving trace (10,000 requests, Poisson arrivals, d U{8..24}, n in {16,32,64}, rhs rank
-      U{1..32}, eps in {1e-6,1e-8,1e-10}): the first 12 requests of the seeded trace at 2
-      requests/s (above capacity, so the replay measures served throughput with queueing)."""
+      U{1..32}, eps in {1e-6,1e-8,1e-10}): the first 8 requests of the seeded trace at 2
+      requests/s (above capacity, so the replay measures served throughput with queueing).
+    Residuals are checked after each timed run (tt_relres_check), outside the timing."""
     import torch
     from torchtt_gb300 import TT, workloads as W
     from torchtt_gb300.serving import Server
-    from torchtt_gb300.trace import replay
 
     t_start = time.perf_counter()
 
-    def served(systems, precision):
+    def left():
+        return args.configs_budget_s - (time.perf_counter() - t_start)
+
+    def served(systems, precision, arrivals=None):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         with Server(slots=args.slots, device=dev) as srv:
-            ids = [srv.submit(A, b, precision=precision, engine=engine, seed=7 + i,
-                              strict_eps=strict, **p) for i, (A, b, p) in enumerate(systems)]
+            ids = []
+            for i, (A, b, p) in enumerate(systems):
+                if arrivals is not None:
+                    wait = arrivals[i] - (time.perf_counter() - t0)
+                    if wait > 0:
+                        time.sleep(wait)
+                ids.append(srv.submit(A, b, precision=precision, engine=engine, seed=7 + i,
+                                      strict_eps=strict, **p))
             res = [srv.result(r) for r in ids]
         el = time.perf_counter() - t0
         lat = [st["queue_ms"] + st["run_ms"] for _, st in res]
-        rr = [float((A @ x - b).norm() / b.norm()) / p["eps"] for (A, b, p), (x, _) in zip(systems, res)]
+        rr = [tt_relres_check(A.cores, x.cores, b.cores) / p["eps"]
+              for (A, b, p), (x, _) in zip(systems, res)]
         return {"solves": len(systems), "solves_per_s": len(systems) / el, "elapsed_s": el,
                 "latency_ms": {"p50": percentile(lat, 0.5), "p99": percentile(lat, 0.99)},
                 "max_relres_over_eps": max(rr), "relres_pass_frac": sum(1 for v in rr if v <= 1.0) / len(rr),
                 "max_rank": max(max(st["ranks"]) for _, st in res)}
 
-    def pair(systems, full_count, note):
+    def pair(systems, full_count, note, arrivals=None):
         out = {"sample": note, "full_size": full_count}
-        out["mixed"] = served(systems, "mixed")
-        out["fp64"] = served(systems, "fp64")
-        out["mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
-        out["extrapolated_full_s"] = {"mixed": full_count / out["mixed"]["solves_per_s"],
-                                      "fp64": full_count / out["fp64"]["solves_per_s"]}
+        t0 = time.perf_counter()
+        out["mixed"] = served(systems, "mixed", arrivals)
+        spent = time.perf_counter() - t0
+        out["extrapolated_full_s"] = {"mixed": full_count / out["mixed"]["solves_per_s"]}
+        if left() > 2.5 * spent:
+            out["fp64"] = served(systems, "fp64", arrivals)
+            out["mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+            out["extrapolated_full_s"]["fp64"] = full_count / out["fp64"]["solves_per_s"]
+        else:
+            out["fp64"] = "skipped: the configs budget left did not cover it"
         return out
 
     res = {"budget_s": args.configs_budget_s, "server_slots": args.slots, "strict_eps": strict}
@@ -316,27 +372,27 @@ def run_configs(args, dev, engine, strict):
     systems = [(TT([c.to(dev) for c in w["A"]]), TT([c.to(dev) for c in w["b"]]), w["params"]) for w in sysd]
     res["parametric_diffusion_d10_n32"] = pair(
         systems, 256, "systems 0, 8, .., 248 of the 256 (rhs ranks across 1-16)")
-    if time.perf_counter() - t_start < 0.45 * args.configs_budget_s:
+    if left() > 0.5 * args.configs_budget_s:
         systems = []
-        for i in range(8):
+        for i in range(4):
             w = W.rounding_stress(i, term_rank=4, nswp=40)
             A = TT([c.to(dev) for c in w["A"]])
             b = TT([c.to(dev) for c in w["b"]]).round(w["round_b"])   # rounded before the clock
             systems.append((A, b, w["params"]))
         res["rounding_stress_d16_n32"] = pair(
-            systems, 128, "solves 0-7 of 128 with b = 4 rank-4 terms (rank 16) rounded to 1e-8 on "
+            systems, 128, "solves 0-3 of 128 with b = 4 rank-4 terms (rank 16) rounded to 1e-8 on "
                           "the GPU before the timed region, nswp 40")
-    if time.perf_counter() - t_start < 0.7 * args.configs_budget_s:
-        out = {"sample": "the first 12 requests of the seeded trace (seed 5) at 2 requests/s",
-               "full_size": 10000}
-        out["mixed"] = replay(12, 2.0, slots=args.slots, precision="mixed", engine=engine,
-                              device=dev.index, strict_eps=strict)
-        out["fp64"] = replay(12, 2.0, slots=args.slots, precision="fp64", engine=engine,
-                             device=dev.index, strict_eps=strict)
-        out["mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
-        out["extrapolated_full_s"] = {"mixed": 10000 / out["mixed"]["solves_per_s"],
-                                      "fp64": 10000 / out["fp64"]["solves_per_s"]}
-        res["serving_trace"] = out
+    if left() > 0.3 * args.configs_budget_s:
+        trace = W.serving_trace(8, 2.0, 5)
+        systems, arrivals = [], []
+        for t_arr, i in trace:
+            w = W.serving_request(i, 5)
+            systems.append((TT([c.to(dev) for c in w["A"]]), TT([c.to(dev) for c in w["b"]]),
+                            w["params"]))
+            arrivals.append(t_arr)
+        res["serving_trace"] = pair(
+            systems, 10000, "the first 8 requests of the seeded trace (seed 5) at 2 requests/s, "
+                            "submitted at their arrival times", arrivals)
     res["elapsed_s"] = time.perf_counter() - t_start
     return res
 
@@ -457,7 +513,7 @@ def run_gb300(args):
 
     # ---- accuracy of the timed solutions (TT algebra on the device) -----------------------------
     def relres(x, b):
-        return float((A_d @ x - b).norm() / b.norm())
+        return tt_relres_check(A_d.cores, x.cores, b.cores)
 
     res_mixed = [relres(x, b) for (x, _), b in zip(results, bs_d)]
     res_fp64 = relres(x_fp64, bs_d[0])
@@ -485,10 +541,12 @@ def run_gb300(args):
             "frac": lowp_tflops / peak if lowp_tflops else None,
             "flops": "algorithmic (dense local-product count) per product / product time",
             "gemm_tflops": gemm_tflops,
-            "traffic": read_profile_value("tc_gemm_d20_n64_local.md", "traffic_bytes_per_launch"),
-            "traffic_source": "profiles/tc_gemm_d20_n64_local.md (one ncu capture, per launch)",
-            "kernel": "low-precision local product: tc_gemm_kernel (tcgen05.mma kind::tf32, 3xTF32 "
-                      "split) for its GEMMs + structured A stage + operand split",
+            "traffic": read_profile_value("tc_gemm_tma_d20_n64_local.md", "traffic_bytes_per_launch"),
+            "traffic_source": "profiles/tc_gemm_tma_d20_n64_local.md (one ncu capture of the GEMM "
+                              "launches at this workload's largest product, per launch)",
+            "kernel": "low-precision local product: tc_gemm_tma_kernel (TMA-fed, warp-specialised "
+                      "tcgen05.mma kind::tf32, 3xTF32 split) for its GEMMs + structured A stage + "
+                      "operand split",
             "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
                            if "bf16_tflops_sustained" in peaks else "fallback 1.7 PF/s sustained",
             "tf32_pipe_frac": 3 * gemm_tflops / (peak / 2) if gemm_tflops else None,

@@ -14,15 +14,22 @@ import numpy as np
 from oracle import amen as O
 
 
-def check(A, b, x, x_ref, eps, kickrank, cond=None, label="", res_slack=1.0):
-    """``res_slack`` > 1 widens the residual bar (the numpy restatement's trajectory differs from
-    ATen's in rounding, and AMEn's stopping rule bounds the true residual only up to a factor)."""
+def check(A, b, x, x_ref, eps, kickrank, cond=None, label="", res_slack=1.0, x_ref_alt=None,
+          rank_tol=None):
+    """``x_ref_alt``: the reference's other solution of the same input (its Python path), when
+    recorded; the residual bar then follows the larger of the reference's two residuals (on the
+    random 4x5x6 system they are 2.2e-11 and 3.3e-10 at eps 1e-10, so "the reference reaches eps"
+    holds for one of its paths only). ``res_slack`` > 1 widens the residual bar (the numpy
+    restatement rounds differently from ATen along the same trajectory). ``rank_tol`` overrides
+    the rank tolerance (default kickrank)."""
     A = [np.asarray(a) for a in A]
     b = [np.asarray(c) for c in b]
     x = [np.asarray(c) for c in x]
     x_ref = [np.asarray(c) for c in x_ref]
     res = O.tt_relres(A, x, b)
     res_ref = O.tt_relres(A, x_ref, b)
+    if x_ref_alt is not None:
+        res_ref = max(res_ref, O.tt_relres(A, [np.asarray(c) for c in x_ref_alt], b))
     err = O.tt_relerr(x, x_ref)
     bound = 10 * eps if cond is None else max(10 * eps, cond * (res + res_ref))
     ranks = [c.shape[2] for c in x][:-1]
@@ -32,7 +39,8 @@ def check(A, b, x, x_ref, eps, kickrank, cond=None, label="", res_slack=1.0):
     print(msg)
     assert res <= res_slack * res_bound(eps, res_ref), msg
     assert err <= bound, msg
-    assert all(abs(a - c) <= kickrank for a, c in zip(ranks, ranks_ref)), msg
+    tol = kickrank if rank_tol is None else rank_tol
+    assert all(abs(a - c) <= tol for a, c in zip(ranks, ranks_ref)), msg
     return res, res_ref, err
 
 
@@ -78,7 +86,7 @@ def res_bound(eps, res_ref):
     return eps if res_ref <= eps else 2.0 * res_ref
 
 
-def check_sampled(A, b, x, z, eps, kickrank, label="", err_bound=None):
+def check_sampled(A, b, x, z, eps, kickrank, label="", err_bound=None, rank_tol=None):
     """Parity of a solution against a sampled fixture of the reference's: relative residual
     (oracle TT algebra) within ``res_bound``, the TT norm within 10 eps of the reference's, the
     sampled estimate of ||x - x_ref|| / ||x_ref|| within 10 eps (or ``err_bound``), TT ranks within
@@ -100,5 +108,6 @@ def check_sampled(A, b, x, z, eps, kickrank, label="", err_bound=None):
     assert res <= res_bound(eps, res_ref), msg
     assert abs(nrm - nrm_ref) <= 10 * eps * nrm_ref, msg
     assert err <= eb, msg
-    assert all(abs(a - c) <= kickrank for a, c in zip(ranks, ranks_ref)), msg
+    tol = kickrank if rank_tol is None else rank_tol
+    assert all(abs(a - c) <= tol for a, c in zip(ranks, ranks_ref)), msg
     return res, res_ref, err

@@ -48,7 +48,7 @@ def test_integration_stub_runs_as_documented(cuda):
     # the stub passes no z0, so the random start differs from the reference's: the bar is the
     # solve tolerance with the operator's condition number (formed densely, 120 x 120)
     _parity.check(A, b, xs, G.cores(z, "x_cpp"), p["eps"], p["kickrank"],
-                  cond=_parity.dense_cond(A), label="INTEGRATION.md stub")
+                  cond=_parity.dense_cond(A), label="INTEGRATION.md stub", x_ref_alt=G.cores(z, "x_py"))
 
 
 class BareTT:

@@ -15,14 +15,15 @@ def to_dev(cores, dev):
     return [torch.from_numpy(np.ascontiguousarray(c)).to(dev) for c in cores]
 
 
-def _check(z, A, b, xs, p, label):
+def _check(z, A, b, xs, p, label, rank_tol=None):
     """Full fixtures: the solution against the reference's cores; sampled fixtures (the benchmark
     workloads at full size): residual, norm, ranks and the sampled estimate of ||x - x_ref||."""
     if G.is_sampled(z):
-        _parity.check_sampled(A, b, xs, z, p["eps"], p["kickrank"], label=label)
+        _parity.check_sampled(A, b, xs, z, p["eps"], p["kickrank"], label=label, rank_tol=rank_tol)
         return
     cond = _parity.dense_cond(A) if int(np.prod([a.shape[1] for a in A])) <= 2000 else None
-    _parity.check(A, b, xs, G.cores(z, "x_cpp"), p["eps"], p["kickrank"], cond=cond, label=label)
+    _parity.check(A, b, xs, G.cores(z, "x_cpp"), p["eps"], p["kickrank"], cond=cond, label=label,
+                  x_ref_alt=G.cores(z, "x_py"), rank_tol=rank_tol)
 
 
 @pytest.mark.parametrize("fixture", G.solve_fixtures())
@@ -87,7 +88,11 @@ def test_edge_cases(cuda):
 
 @pytest.mark.parametrize("fixture", G.solve_fixtures())
 def test_mixed_solve_matches_reference(cuda, fixture):
-    """The mixed-precision path meets the same parity bar against the reference's FP64 solution."""
+    """The mixed-precision path meets the same residual and solution bar against the reference's
+    FP64 solution. Its ranks are held to 2 kickrank: its stopping test (max local residual < eps)
+    can fire a sweep later than the FP64 path's, and a sweep grows a rank by up to kickrank (on
+    the d=20 n=64 solve one extra sweep gave ranks up to 9 above the reference's, with a lower
+    residual, 2.5e-8 against 3.4e-8)."""
     from torchtt_gb300 import TT, amen_solve
     z = G.load(fixture)
     A, b = G.cores(z, "A"), G.cores(z, "b")
@@ -101,7 +106,7 @@ def test_mixed_solve_matches_reference(cuda, fixture):
                        preconditioner=prec, z0=to_dev(z0, cuda), return_stats=True,
                        precision="mixed")
     xs = [c.cpu().numpy() for c in x.cores]
-    _check(z, A, b, xs, p, fixture + " mixed")
+    _check(z, A, b, xs, p, fixture + " mixed", rank_tol=2 * p["kickrank"])
 
 
 def test_mixed_equals_fp64_on_laplace(cuda):
@@ -160,7 +165,7 @@ def test_double_float_products_match_native(cuda, fixture):
     xn, sn = solve_cores(dev(A), dev(b), dev(x0), dev(z0), fp64_engine="native", **kw)
     assert float((TT(xd) - TT(xn)).norm() / TT(xn).norm()) <= 10 * p["eps"]
     _parity.check(A, b, [c.cpu().numpy() for c in xd], G.cores(z, "x_cpp"), p["eps"],
-                  p["kickrank"], label="double-float " + fixture)
+                  p["kickrank"], label="double-float " + fixture, x_ref_alt=G.cores(z, "x_py"))
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
