@@ -697,7 +697,7 @@ def main():
     ap.add_argument("--fp64-solves", type=int, default=2)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--configs-budget-s", type=float, default=150.0,
+    ap.add_argument("--configs-budget-s", type=float, default=180.0,
                     help="wall budget of the batched/served workloads block (0: skip it)")
     ap.add_argument("--strict-eps", action="store_true",
                     help="solve every system to a true relres <= eps (strict_eps: AMEn at eps / 4); "
