@@ -572,8 +572,6 @@ int64_t autotune_classes() {
 NoTuningScope::NoTuningScope() : prev_(t_no_tuning_runs) { t_no_tuning_runs = true; }
 NoTuningScope::~NoTuningScope() { t_no_tuning_runs = prev_; }
 
-int fp64_engine() { return t_fp64_engine; }
-
 Fp64EngineScope::Fp64EngineScope(int engine) : prev_(t_fp64_engine) { t_fp64_engine = engine; }
 Fp64EngineScope::~Fp64EngineScope() { t_fp64_engine = prev_; }
 

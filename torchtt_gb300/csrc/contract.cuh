@@ -47,9 +47,6 @@ using ContractDescF = ContractDescT<float>;
 // operands within the FP32 exponent range). Set for a scope with Fp64EngineScope.
 constexpr int kFp64Native = 0;
 constexpr int kFp64DoubleFloat = 1;
-// The calling thread's current engine of FP64 contractions (kFp64Native or kFp64DoubleFloat); the
-// mixed path's CholeskyQR also runs its Cholesky factorisation in double-float under the latter.
-int fp64_engine();
 struct Fp64EngineScope {
   explicit Fp64EngineScope(int engine);
   ~Fp64EngineScope();

@@ -1,6 +1,6 @@
-// Double-float arithmetic on the FP32 pipe: a value is an unevaluated pair hi + lo of FP32 numbers
-// (~48 significant bits). Used where GB300's FP64 pipe (1/60 of its FP32 rate) would bound a kernel
-// and ~1e-14 relative accuracy per operation suffices.
+// The FP64 -> double-float split of the double-float contraction engine: a value becomes an
+// unevaluated pair hi + lo of FP32 numbers (~48 significant bits), so products and sums run on the
+// FP32 pipe, GB300's FP64 pipe being 1/60 of its FP32 rate.
 #pragma once
 
 #include <cstdint>
@@ -35,98 +35,5 @@ __device__ __forceinline__ void df_split(double x, float& h, float& l) {
   }
 }
 
-
-struct Df {
-  float h, l;
-};
-
-__device__ __forceinline__ Df df_of(double x) {
-  Df r;
-  df_split(x, r.h, r.l);
-  return r;
-}
-
-__device__ __forceinline__ double df_to_double(Df a) { return (double)a.h + (double)a.l; }
-
-// error-free product a.h * b.h plus the cross terms: (p, e) with a b = p + e to ~2^-48
-__device__ __forceinline__ void df_prod(Df a, Df b, float& p, float& e) {
-  p = a.h * b.h;
-  e = fmaf(a.h, b.h, -p);
-  e = fmaf(a.h, b.l, e);
-  e = fmaf(a.l, b.h, e);
-}
-
-// c - a b, renormalised
-__device__ __forceinline__ Df df_fms(Df c, Df a, Df b) {
-  float p, e;
-  df_prod(a, b, p, e);
-  const float s = c.h - p;
-  const float bb = s - c.h;
-  const float err = (c.h - (s - bb)) + (-p - bb);
-  const float lo = (c.l - e) + err;
-  Df r;
-  r.h = s + lo;
-  r.l = lo - (r.h - s);
-  return r;
-}
-
-// a b, renormalised
-__device__ __forceinline__ Df df_mul(Df a, Df b) {
-  float p, e;
-  df_prod(a, b, p, e);
-  Df r;
-  r.h = p + e;
-  r.l = e - (r.h - p);
-  return r;
-}
-
-// A double-float number with arithmetic operators, for templates written over a value type T
-// (the cluster Jacobi): + - * and fma renormalise their result; comparisons and the conversion to
-// double evaluate hi + lo in FP64.
-struct DfN {
-  float h, l;
-  DfN() = default;
-  __device__ __forceinline__ explicit DfN(double x) { df_split(x, h, l); }
-  __device__ __forceinline__ explicit DfN(int x) : h((float)x), l(0.f) {}
-  __device__ __forceinline__ static DfN make(float hi, float lo) {
-    DfN r;
-    r.h = hi;
-    r.l = lo;
-    return r;
-  }
-  __device__ __forceinline__ explicit operator double() const { return (double)h + (double)l; }
-};
-
-__device__ __forceinline__ DfN operator+(DfN a, DfN b) {
-  const float s = a.h + b.h;
-  const float bb = s - a.h;
-  const float err = (a.h - (s - bb)) + (b.h - bb);
-  const float lo = err + (a.l + b.l);
-  const float h = s + lo;
-  return DfN::make(h, lo - (h - s));
-}
-__device__ __forceinline__ DfN operator-(DfN a) { return DfN::make(-a.h, -a.l); }
-__device__ __forceinline__ DfN operator-(DfN a, DfN b) { return a + (-b); }
-__device__ __forceinline__ DfN operator*(DfN a, DfN b) {
-  float p, e;
-  df_prod(Df{a.h, a.l}, Df{b.h, b.l}, p, e);
-  const float h = p + e;
-  return DfN::make(h, e - (h - p));
-}
-// the FP64 and FP32 fma stay visible beside the double-float one inside this namespace
-using ::fma;
-
-// c + a b
-__device__ __forceinline__ DfN fma(DfN a, DfN b, DfN c) {
-  float p, e;
-  df_prod(Df{a.h, a.l}, Df{b.h, b.l}, p, e);
-  const float s = c.h + p;
-  const float bb = s - c.h;
-  const float err = (c.h - (s - bb)) + (p - bb);
-  const float lo = (c.l + e) + err;
-  const float h = s + lo;
-  return DfN::make(h, lo - (h - s));
-}
-__device__ __forceinline__ bool operator>(DfN a, DfN b) { return (double)a > (double)b; }
 
 }  // namespace ttgb

@@ -12,7 +12,6 @@
 #include <cmath>
 
 #include "contract.cuh"
-#include "df.cuh"
 #include "linalg.cuh"
 
 namespace cg = cooperative_groups;
@@ -215,116 +214,6 @@ __global__ void __launch_bounds__(512) chol_inv_smem_kernel(const double* __rest
         Riout[i * n + k] = X[i * ld + k];
       }
   }
-}
-
-// The same fused Cholesky + triangular inverse in double-float arithmetic on the FP32 pipe (~48
-// significant bits per operation), for the CholeskyQR3 of the mixed path whose Gram products are
-// already double-float: on GB300 one SM issues ~2 FP64 FMA per clock against 128 FP32, and the
-// n^3/3 + n^3/3 multiply-adds of this single-block kernel are its whole cost. The matrix is
-// scaled by a power of two (largest diagonal entry to [1, 4)) before the split, so every entry
-// lies inside the FP32 exponent range; the pivots' square roots and reciprocals are computed in
-// FP64 by one thread. Same shift, identity check and status semantics as chol_inv_smem_kernel.
-__global__ void __launch_bounds__(512) chol_inv_df_kernel(const double* __restrict__ Gin, int n,
-                                                          int64_t shift_rows, int check_identity,
-                                                          double* Rout, double* Riout, int* status) {
-  extern __shared__ float smf[];
-  const int ld = n + 1;
-  Df* G = reinterpret_cast<Df*>(smf);   // becomes R (upper)
-  Df* X = G + n * ld;                   // becomes R^{-1} (upper)
-  __shared__ double sh[32];
-  __shared__ int bad;
-  __shared__ double scale_sh, shift_sh;
-  __shared__ Df piv_sh, inv_sh;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  if (tid == 0) bad = 0;
-  double mx = 0.0, tr = 0.0;
-  for (int i = tid; i < n; i += nt) {
-    const double g = Gin[(int64_t)i * n + i];
-    mx = fmax(mx, fabs(g));
-    tr += g;
-  }
-  mx = block_max_d(mx, sh);
-  tr = block_sum_d(tr, sh);
-  if (check_identity) {
-    double dev = 0.0;
-    for (int t = tid; t < n * n; t += nt) {
-      const int i = t / n, k = t % n;
-      if (k < i) continue;   // the Gram matrix is formed (and read) in its upper triangle only
-      const double v = Gin[t] - (i == k ? 1.0 : 0.0);
-      dev = fmax(dev, isfinite(v) ? fabs(v) : 1e300);
-    }
-    dev = block_max_d(dev, sh);
-    if (tid == 0 && !(dev <= 0.1)) *status = 2;
-  }
-  if (tid == 0) {
-    // power-of-two scale: the largest diagonal entry to [1, 4), so R scales by 2^-e exactly
-    const int e = (mx > 0.0 && isfinite(mx)) ? (ilogb(mx) >> 1) : 0;
-    scale_sh = ldexp(1.0, -2 * e);
-    shift_sh = shift_rows > 0 ? 11.0 * ((double)shift_rows * n + (double)n * (n + 1)) * kEps * tr : 0.0;
-  }
-  __syncthreads();
-  const double sc = scale_sh, sft = shift_sh;
-  for (int t = tid; t < n * n; t += nt) {
-    const int i = t / n, k = t % n;
-    const double g = (Gin[t] + (i == k ? sft : 0.0)) * sc;
-    G[i * ld + k] = df_of(g);
-  }
-  __syncthreads();
-  for (int j = 0; j < n; ++j) {
-    if (tid == 0) {
-      const double d = df_to_double(G[j * ld + j]);
-      if (!(d > 0.0) || !isfinite(d)) { bad = 1; *status = 1; }
-      else {
-        const double rd = sqrt(d);
-        piv_sh = df_of(rd);
-        inv_sh = df_of(1.0 / rd);
-      }
-    }
-    __syncthreads();
-    if (bad) break;
-    const Df inv = inv_sh;
-    if (tid == 0) G[j * ld + j] = piv_sh;
-    for (int k = j + 1 + tid; k < n; k += nt) G[j * ld + k] = df_mul(G[j * ld + k], inv);
-    __syncthreads();
-    for (int i = j + 1 + warp; i < n; i += nw) {   // trailing update of the upper triangle
-      const Df gji = G[j * ld + i];
-      Df* gi = G + i * ld;
-      const Df* gj = G + j * ld;
-      for (int k = i + lane; k < n; k += 32) gi[k] = df_fms(gi[k], gji, gj[k]);
-    }
-    __syncthreads();
-  }
-  if (bad) return;
-  const Df zero = {0.f, 0.f}, one = {1.f, 0.f};
-  for (int i = warp; i < n; i += nw)
-    for (int k = lane; k < n; k += 32) {
-      if (k < i) G[i * ld + k] = zero;
-      X[i * ld + k] = (k == i) ? one : zero;
-    }
-  __syncthreads();
-  // X = R^{-1} by back substitution on the identity (row j of X final after scaling)
-  for (int j = n - 1; j >= 0; --j) {
-    if (tid == 0) inv_sh = df_of(1.0 / df_to_double(G[j * ld + j]));
-    __syncthreads();
-    const Df inv = inv_sh;
-    for (int k = j + tid; k < n; k += nt) X[j * ld + k] = df_mul(X[j * ld + k], inv);
-    __syncthreads();
-    for (int i = warp; i < j; i += nw) {
-      const Df gij = G[i * ld + j];
-      Df* xi = X + i * ld;
-      const Df* xj = X + j * ld;
-      for (int k = j + lane; k < n; k += 32) xi[k] = df_fms(xi[k], gij, xj[k]);
-    }
-    __syncthreads();
-  }
-  // undo the scale: G' = s G -> R' = sqrt(s) R, so R = R' / sqrt(s) and R^{-1} = sqrt(s) R'^{-1}
-  const double rs = sqrt(sc);
-  for (int i = warp; i < n; i += nw)
-    for (int k = lane; k < n; k += 32) {
-      Rout[i * n + k] = df_to_double(G[i * ld + k]) / rs;
-      Riout[i * n + k] = df_to_double(X[i * ld + k]) * rs;
-    }
 }
 
 // Ri = R^{-1} for the upper-triangular row-major R (one thread per column of Ri).
@@ -574,33 +463,6 @@ __device__ __forceinline__ bool jacobi_rotation(double a, double b, double g, do
 
 __device__ __forceinline__ double warp_sum_t(double v) { return warp_sum_d(v); }
 
-__device__ __forceinline__ DfN warp_sum_t(DfN v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
-    v = v + DfN::make(__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o));
-  return v;
-}
-
-// The rotation of a double-float sweep: angle and cosine from the FP64 values of the pair's
-// norms and inner product (the same formula as the FP64 sweep), rounded to double-float.
-__device__ __forceinline__ bool jacobi_rotation(DfN a, DfN b, DfN g, DfN tol, DfN& c, DfN& s) {
-  double cd, sd;
-  if (!jacobi_rotation((double)a, (double)b, (double)g, (double)tol, cd, sd)) return false;
-  c = DfN(cd);
-  s = DfN(sd);
-  return true;
-}
-
-// convergence threshold of a sweep: n units of the arithmetic's precision (FP64, or double-float
-// whose ~48-bit operations cannot drive an inner product below ~n 2^-48 of the norms)
-template <typename T> __device__ __forceinline__ T jacobi_tol(int n) { return T(n > 1 ? n : 1) * T(kEps); }
-template <> __device__ __forceinline__ float jacobi_tol<float>(int n) { return (float)(n > 1 ? n : 1) * 1.1920929e-7f; }
-template <> __device__ __forceinline__ DfN jacobi_tol<DfN>(int n) { return DfN((double)(n > 1 ? n : 1) * 0x1p-44); }
-
-// value type <-> storage type of the Jacobi kernels' global input and output
-template <typename T> __device__ __forceinline__ T to_val(double x) { return T(x); }
-template <typename T> __device__ __forceinline__ double to_store(T x) { return (double)x; }
-
 __device__ __forceinline__ int rr_index(int p, int r, int nn) {
   return p == 0 ? 0 : ((p - 1 + r) % (nn - 1)) + 1;
 }
@@ -753,8 +615,8 @@ __device__ __forceinline__ int jacobi_rotate_tracked(T* wp, T* wq, T* vp, T* vq,
 
 template <typename T>
 __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
-    jacobi_block_kernel(const double* __restrict__ Win, int n, double* Wout, double* Vout,
-                        int max_sweeps, int* status, const double* __restrict__ Vin) {
+    jacobi_block_kernel(const T* __restrict__ Win, int n, T* Wout, T* Vout, int max_sweeps,
+                        int* status, const T* __restrict__ Vin) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
   T* sm = reinterpret_cast<T*>(sm_raw);
   cg::cluster_group cluster = cg::this_cluster();
@@ -771,7 +633,7 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
   __shared__ int local_cnt;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  const T tol = jacobi_tol<T>(n);
+  const T tol = T(n > 1 ? n : 1) * (sizeof(T) == 8 ? T(kEps) : T(1.1920929e-7f));
   // round 0 of sweep 0: slot 0 holds block rank, slot 1 block P-1-rank
   for (int sl = 0; sl < 2; ++sl) {
     const int b = sl == 0 ? rank : P - 1 - rank;
@@ -780,8 +642,8 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
     for (int64_t t = tid; t < blk; t += nt) {
       const int j = (int)(t / n), i = (int)(t - (int64_t)j * n);
       const int c = b * nb + j;
-      W[t] = (c < n) ? to_val<T>(Win[(int64_t)c * n + i]) : T(0);
-      V[t] = (c < n) ? (Vin ? to_val<T>(Vin[(int64_t)c * n + i]) : (i == c ? T(1) : T(0))) : T(0);
+      W[t] = (c < n) ? Win[(int64_t)c * n + i] : T(0);
+      V[t] = (c < n) ? (Vin ? Vin[(int64_t)c * n + i] : (i == c ? T(1) : T(0))) : T(0);
     }
   }
   int* counts0 = cluster.map_shared_rank(counts, 0);
@@ -879,8 +741,8 @@ __global__ void __cluster_dims__(kJacobiCluster, 1, 1) __launch_bounds__(256)
       const int j = (int)(t / n), i = (int)(t - (int64_t)j * n);
       const int c = b * nb + j;
       if (c < n) {
-        Wout[(int64_t)c * n + i] = to_store<T>(W[t]);
-        Vout[(int64_t)c * n + i] = to_store<T>(V[t]);
+        Wout[(int64_t)c * n + i] = W[t];
+        Vout[(int64_t)c * n + i] = V[t];
       }
     }
   }
@@ -1191,14 +1053,7 @@ QRResult qr(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, doubl
   for (int pass = 0; pass < 3; ++pass) {
     // Gram matrix: only its lower (column-major) = upper (row-major) triangle is formed and read
     gemm_cm(Ain, ldin, Ain, ldin, G, n, n, n, m, 1.0, 0.0, s, true, false, kTriLowerC);
-    if (n <= kCholSmemMax && fp64_engine() == kFp64DoubleFloat) {
-      const size_t smem = (size_t)2 * n * (n + 1) * sizeof(Df);
-      smem_optin((const void*)chol_inv_df_kernel,
-                 (int)(2 * kCholSmemMax * (kCholSmemMax + 1) * sizeof(Df)));
-      chol_inv_df_kernel<<<1, 512, smem, s>>>(G, (int)n, pass == 0 ? m : 0, pass == 2 ? 1 : 0, G,
-                                              Ri, ws.status);
-      TTGB_CHECK_LAUNCH();
-    } else if (n <= kCholSmemMax) {
+    if (n <= kCholSmemMax) {
       const size_t smem = (size_t)2 * n * (n + 1) * sizeof(double);
       smem_optin((const void*)chol_inv_smem_kernel,
                  (int)(2 * kCholSmemMax * (kCholSmemMax + 1) * sizeof(double)));
@@ -1263,17 +1118,9 @@ void svd(const double* A, int64_t lda, int64_t m, int64_t n, double* U, double* 
     const int nb = (int)((n + 2 * kJacobiCluster - 1) / (2 * kJacobiCluster));
     const int64_t unit = 2 * nb * n + nb + (nb & 1);
     const size_t smem = (size_t)4 * unit * sizeof(double);
-    if (fp64_engine() == kFp64DoubleFloat) {
-      // the mixed path's sweeps in double-float on the FP32 pipe (see jacobi_tol)
-      static_assert(sizeof(DfN) == sizeof(double), "double-float values take a double's place");
-      smem_optin((const void*)jacobi_block_kernel<DfN>, (int)smem);
-      jacobi_block_kernel<DfN><<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status,
-                                                                 nullptr);
-    } else {
     smem_optin((const void*)jacobi_block_kernel<double>, (int)smem);
     jacobi_block_kernel<double><<<kJacobiCluster, 256, smem, s>>>(W, (int)n, W, Vw, 60, ws.status,
                                                                   nullptr);
-    }
     TTGB_CHECK_LAUNCH();
     DBuf sig((size_t)n, s);
     svd_sort_kernel<<<1, 1024, 0, s>>>(W, Vw, (int)n, Up.p, S, Vw + n * n, sig.p);
