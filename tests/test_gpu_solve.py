@@ -151,7 +151,10 @@ def test_structured_a_matches_dense(cuda, precision):
 @pytest.mark.parametrize("fixture", ["solve_laplace_d8_n16.npz", "solve_random_4x5x6.npz"])
 def test_double_float_products_match_native(cuda, fixture):
     """The mixed path's FP64 products in double-float arithmetic on the FP32 pipe (default) give
-    the solution of the native-FP64 products within the solve tolerance, and the reference's."""
+    the solution of the native-FP64 products within the solve tolerance, and the reference's. The
+    two solves share z0 but not every rounding, so their difference is held to the bar of the
+    parity checks: 10 eps, or cond(A) (relres_df + relres_native) where the operator can be formed
+    (the random 4x5x6 system has cond 2.3e3 and relres ~3 eps at eps 1e-10)."""
     from torchtt_gb300 import TT
     from torchtt_gb300.solvers import solve_cores
     z = G.load(fixture)
@@ -163,7 +166,12 @@ def test_double_float_products_match_native(cuda, fixture):
               preconditioner=int(z["prec"]))
     xd, sd = solve_cores(dev(A), dev(b), dev(x0), dev(z0), fp64_engine="df", **kw)
     xn, sn = solve_cores(dev(A), dev(b), dev(x0), dev(z0), fp64_engine="native", **kw)
-    assert float((TT(xd) - TT(xn)).norm() / TT(xn).norm()) <= 10 * p["eps"]
+    from oracle import amen as O
+    xdn, xnn = [c.cpu().numpy() for c in xd], [c.cpu().numpy() for c in xn]
+    bound = 10 * p["eps"]
+    if int(np.prod([a.shape[1] for a in A])) <= 2000:
+        bound = max(bound, _parity.dense_cond(A) * (O.tt_relres(A, xdn, b) + O.tt_relres(A, xnn, b)))
+    assert float((TT(xd) - TT(xn)).norm() / TT(xn).norm()) <= bound
     _parity.check(A, b, [c.cpu().numpy() for c in xd], G.cores(z, "x_cpp"), p["eps"],
                   p["kickrank"], label="double-float " + fixture, x_ref_alt=G.cores(z, "x_py"))
 

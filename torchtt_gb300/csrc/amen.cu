@@ -388,13 +388,21 @@ void AmenRun::backward_step(int k, int swp, bool last) {
       axpby(-1.0, czA.p, 1.0, czy.p, rz_[k] * X, s_);   // czy*nrmsc - czA
       // right singular vectors of the rz_k x X matrix == left ones of its column-major view
       const int64_t kf = rz_[k] < X ? rz_[k] : X;
-      DBuf U((size_t)(X * kf), s_), S((size_t)kf, s_), Vh((size_t)(kf * rz_[k]), s_);
-      svd(czy.p, X, X, rz_[k], U.p, S.p, Vh.p, lws_, red_, s_);
       const int64_t tk = p_.kickrank < kf ? p_.kickrank : kf;
       kc = tk + ((k < d_ - 1) ? p_.kick2 : 0);
-      czm.reset((size_t)(X * kc), s_);
-      copy(U.p, czm.p, X * tk, s_);
-      if (kc > tk) randn_fill(czm.p + X * tk, X * (kc - tk));
+      if (kc == kf && kf == rz_[k]) {
+        // every singular vector is kept and nothing is appended: the new z directions span the
+        // column space of czy, and only that span enters the enrichment and the z interfaces, so
+        // the QR below orthonormalises czy itself (the SVD would only order a basis of the same
+        // span)
+        czm = std::move(czy);
+      } else {
+        DBuf U((size_t)(X * kf), s_), S((size_t)kf, s_), Vh((size_t)(kf * rz_[k]), s_);
+        svd(czy.p, X, X, rz_[k], U.p, S.p, Vh.p, lws_, red_, s_);
+        czm.reset((size_t)(X * kc), s_);
+        copy(U.p, czm.p, X * tk, s_);
+        if (kc > tk) randn_fill(czm.p + X * tk, X * (kc - tk));
+      }
     } else {
       kc = rz_[k];
       czm.reset((size_t)(X * kc), s_);
@@ -862,14 +870,20 @@ void AmenRun::z_update_forward(int k, const double* trunc) {
   lrhs(Phiz_b_[k].data(), rz_[k], k, Phiz_b_[k + 1].data(), rz_[k + 1], nrmsc_, czy.p);
   axpby(-1.0, czA.p, 1.0, czy.p, ap * bp, s_);
   const int64_t kf = ap < bp ? ap : bp;
-  DBuf Mc((size_t)(ap * bp), s_), U((size_t)(ap * kf), s_), S((size_t)kf, s_), Vh((size_t)(kf * bp), s_);
+  DBuf Mc((size_t)(ap * bp), s_);
   transpose(czy.p, bp, Mc.p, ap, bp, ap, s_);
-  svd(Mc.p, ap, ap, bp, U.p, S.p, Vh.p, lws_, red_, s_);
   const int64_t tk = p_.kickrank < kf ? p_.kickrank : kf;
   const int64_t kc = tk + ((k < d_ - 1) ? p_.kick2 : 0);
-  DBuf cz((size_t)(ap * kc), s_);
-  copy(U.p, cz.p, ap * tk, s_);
-  if (kc > tk) randn_fill(cz.p + ap * tk, ap * (kc - tk));
+  DBuf cz;
+  if (kc == kf && kf == bp) {   // all singular vectors kept, none appended: orthonormalise Mc
+    cz = std::move(Mc);
+  } else {
+    DBuf U((size_t)(ap * kf), s_), S((size_t)kf, s_), Vh((size_t)(kf * bp), s_);
+    svd(Mc.p, ap, ap, bp, U.p, S.p, Vh.p, lws_, red_, s_);
+    cz.reset((size_t)(ap * kc), s_);
+    copy(U.p, cz.p, ap * tk, s_);
+    if (kc > tk) randn_fill(cz.p + ap * tk, ap * (kc - tk));
+  }
   const int64_t k3 = ap < kc ? ap : kc;
   DBuf qz((size_t)(ap * k3), s_), Rz((size_t)(k3 * kc), s_);
   qr(cz.p, ap, ap, kc, qz.p, Rz.p, lws_, red_, s_);
