@@ -387,10 +387,20 @@ bool overlaps(const T* x, int64_t xs, const T* y, int64_t ys) {
   return x < y + ys + 1 && y < x + xs + 1;
 }
 
+// CTAs a split-K launch aims at, in multiples of the SM count (TTGB_SPLIT_TARGET, default 2)
+double split_target() {
+  static const double v = [] {
+    const char* e = std::getenv("TTGB_SPLIT_TARGET");
+    const double x = e ? std::atof(e) : 2.0;
+    return (x > 0.0 && x <= 16.0) ? x : 2.0;
+  }();
+  return v;
+}
+
 template <typename T>
 int heuristic_split(const ContractDescT<T>& d, int bm, int bn, int sms, bool force) {
   const int64_t t = (int64_t)cdiv(d.M, bm) * cdiv(d.N, bn) * d.batch;
-  const int64_t target = 2 * (int64_t)sms;
+  const int64_t target = (int64_t)(split_target() * sms);
   if (!force && !(t < sms && d.K >= 128)) return 1;
   int splitk = (int)((target + t - 1) / t);
   const int maxsplit = d.K / 64;
