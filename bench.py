@@ -567,18 +567,21 @@ def run_gb300(args):
         "share_of_solve": pm["lowp_ms"] / max(1e-9, sum(pm["phase_ms"].values())),
     })
     fp64_tflops = pf["contract_flops"] / (pf["contract_ms"] * 1e-3) / 1e12 if pf["contract_ms"] > 0 else None
-    # Krylov orthogonalisation (multidot + two gs_update per GMRES iteration) against HBM: the
+    # Krylov orthogonalisation (three Arnoldi launches per GMRES iteration) against HBM: the
     # reference's algorithmic bytes 8 N_loc (2k + 3) per iteration / the kernels' event time, and
-    # the bytes the CGS2 kernels actually move; the basis (<= 41 vectors of N_loc doubles, ~125 MB
-    # at the largest local problem) is mostly L2-resident, so HBM is an upper bound of the rate
+    # the bytes the Arnoldi kernels actually move; the basis (<= 41 vectors of N_loc doubles,
+    # ~125 MB at the largest local problem) is mostly L2-resident, so HBM bounds the rate
     kms = pm.get("krylov_ms", 0.0)
     hbm = peaks.get("hbm_gbs") or 6800.0
-    kry = {"kernels": "multidot_kernel + 2x gs_update_kernel per GMRES iteration (mixed path)",
+    kry = {"kernels": "arnoldi_project + arnoldi_reorth + arnoldi_finish per GMRES iteration "
+                      "(mixed path)",
            "bound": "hbm", "unit": "GB/s", "peak": hbm,
            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks
                           else "fallback 6.8 TB/s",
            "achieved": pm["krylov_bytes"] / (kms * 1e-3) / 1e9 if kms > 0 else None,
            "moved_gbs": pm["krylov_traffic_bytes"] / (kms * 1e-3) / 1e9 if kms > 0 else None,
+           "moved_over_algorithmic": (pm["krylov_traffic_bytes"] / pm["krylov_bytes"]
+                                      if pm.get("krylov_bytes") else None),
            "ms": kms, "launches": pm.get("krylov_launches"),
            "avg_launch_us": 1000 * kms / max(1, pm.get("krylov_launches", 0))}
     kry["frac"] = kry["achieved"] / hbm if kry["achieved"] else None
@@ -664,7 +667,10 @@ def run_gb300(args):
                                      else "the reference's rule (max local residual < eps)"},
             "solve": {"sweeps": mixed_stats["sweeps"], "max_rank": max(mixed_stats["ranks"]),
                       "gmres_iterations": mixed_stats["gmres_iterations"],
-                      "host_syncs": mixed_stats["host_syncs"]},
+                      "host_syncs": mixed_stats["host_syncs"],
+                      "gmres_syncs": mixed_stats.get("gmres_syncs"),
+                      "gmres_overrun": mixed_stats.get("gmres_overrun"),
+                      "gmres_reorth": mixed_stats.get("gmres_reorth")},
             "server": {"peak_running": srv_stats.get("peak_running"), "completed": srv_stats.get("completed")},
             "roofline": roofline,
             "fp64_contract_roofline": fp64_roof,

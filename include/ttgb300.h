@@ -122,7 +122,12 @@ typedef struct ttgb_stats {
   double krylov_bytes;          /* profile: algorithmic bytes of those iterations, 8 N_loc (2k + 3)
                                    for iteration k (the reference's MGS reads k + 1 vectors twice
                                    and writes one) */
-  double krylov_traffic_bytes;  /* profile: bytes the CGS2 kernels read and write, 8 N_loc (4k + 10) */
+  double krylov_traffic_bytes;  /* profile: bytes the Arnoldi kernels read and write: 8 N_loc (2k + 7)
+                                   for iteration k, plus 8 N_loc (k + 1) when it takes the second
+                                   projection */
+  int64_t gmres_syncs;          /* host reads of the GMRES stop flag (also counted in host_syncs) */
+  int64_t gmres_overrun;        /* GMRES iterations queued past their cycle's stopping point */
+  int64_t gmres_reorth;         /* GMRES iterations that took the second projection */
 } ttgb_stats;
 
 typedef struct ttgb_solution ttgb_solution;   /* opaque, library-owned result */

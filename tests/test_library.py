@@ -39,7 +39,7 @@ def test_ctypes_binding_covers_the_header(built):
     from torchtt_gb300 import _lib
     assert sorted(_lib.EXPORTED) == declared_symbols()
     L = _lib.lib()
-    assert L.ttgb_version() == 102
+    assert L.ttgb_version() == 103
     p = _lib.AmenParams()
     L.ttgb_default_params(p)
     # defaults of torchtt/solvers.py:211

@@ -45,7 +45,8 @@ class Stats(ctypes.Structure):
                 ("lowp_matvecs", c_i64), ("lowp_flops", c_dbl), ("refinements", c_i64),
                 ("phase_ms", c_dbl * 12), ("lowp_ms", c_dbl), ("lowp_launches", c_i64),
                 ("lowp_gemm_flops", c_dbl), ("krylov_ms", c_dbl), ("krylov_launches", c_i64),
-                ("krylov_bytes", c_dbl), ("krylov_traffic_bytes", c_dbl)]
+                ("krylov_bytes", c_dbl), ("krylov_traffic_bytes", c_dbl),
+                ("gmres_syncs", c_i64), ("gmres_overrun", c_i64), ("gmres_reorth", c_i64)]
 
     PHASES = ("bwd_z", "bwd_qr", "bwd_phi", "fwd_setup", "local_solve", "svd", "rank_search",
               "fwd_z", "enrichment", "fwd_phi", "other")

@@ -92,15 +92,15 @@ class AmenRun {
     N_ = A.cols;
     rA_ = A.ranks;
     rb_ = b.ranks;
-    red_partial_.reset(512 * 128, s_);
+    red_partial_.reset(1024 * 128, s_);
     TTGB_CUDA(cudaMallocAsync((void**)&red_counter_, 64, s_));
     TTGB_CUDA(cudaMemsetAsync(red_counter_, 0, 64, s_));
     red_.partial = red_partial_.p;
     red_.counter = red_counter_;
-    red_.cap_blocks = 512;
+    red_.cap_blocks = 1024;
     red_.cap_vec = 127;
     TTGB_CUDA(cudaMallocAsync((void**)&lws_.status, 16, s_));
-    TTGB_CUDA(cudaMallocAsync((void**)&gws_.d_flag, 16, s_));
+    TTGB_CUDA(cudaMallocAsync((void**)&gws_.d_flag, 32, s_));
     TTGB_CUDA(cudaMemsetAsync(lws_.status, 0, 16, s_));
     TTGB_CUDA(cudaMallocHost((void**)&hbuf_, 4096));
     lws_.h_status = (int*)hbuf_;
@@ -176,6 +176,13 @@ class AmenRun {
   std::unique_ptr<PhaseTimer> phases_;
   void phase(int p) {
     if (phases_) phases_->mark(p);
+  }
+
+  void note_gmres(const GmresResult& gr) {
+    st_.gmres_syncs += gr.syncs;
+    st_.host_syncs += gr.syncs;
+    st_.gmres_overrun += gr.overrun;
+    st_.gmres_reorth += gr.reorth;
   }
 
   void read_scalars(int n) {
@@ -439,17 +446,20 @@ void AmenRun::backward_step(int k, int swp, bool last) {
   phi_A(false, Phis_[k + 1], x_[k].data(), rx_[k], rx_[k + 1], x_[k].data(), rx_[k], rx_[k + 1], k,
         Phis_[k]);
   phi_b(false, Phis_b_[k + 1], x_[k].data(), rx_[k], rx_[k + 1], k, Phis_b_[k]);
-  nrm2(red_, Phis_[k].data(), Phis_[k].numel(), slot(kNormPhi), s_);
-  nrm2(red_, Phis_b_[k].data(), Phis_b_[k].numel(), slot(kNormPhiB), s_);
-  scale_dev(Phis_[k].data(), Phis_[k].numel(), nullptr, slot(kNormPhi), s_);
-  scale_dev(Phis_b_[k].data(), Phis_b_[k].numel(), nullptr, slot(kNormPhiB), s_);
+  nrm2_multi(red_, VecSegs()
+                         .norm(Phis_[k].data(), Phis_[k].numel(), slot(kNormPhi))
+                         .norm(Phis_b_[k].data(), Phis_b_[k].numel(), slot(kNormPhiB)), s_);
+  VecSegs scl;
+  scl.scale(Phis_[k].data(), Phis_[k].numel(), slot(kNormPhi))
+      .scale(Phis_b_[k].data(), Phis_b_[k].numel(), slot(kNormPhiB));
   if (!last) {   // amen_solve.h:288-291
     phi_A(false, Phiz_[k + 1], z_[k].data(), rz_[k], rz_[k + 1], x_[k].data(), rx_[k], rx_[k + 1],
           k, Phiz_[k]);
     phi_b(false, Phiz_b_[k + 1], z_[k].data(), rz_[k], rz_[k + 1], k, Phiz_b_[k]);
-    scale_dev(Phiz_[k].data(), Phiz_[k].numel(), nullptr, slot(kNormPhi), s_);
-    scale_dev(Phiz_b_[k].data(), Phiz_b_[k].numel(), nullptr, slot(kNormPhiB), s_);
+    scl.scale(Phiz_[k].data(), Phiz_[k].numel(), slot(kNormPhi))
+        .scale(Phiz_b_[k].data(), Phiz_b_[k].numel(), slot(kNormPhiB));
   }
+  scale_multi(scl, s_);
   read_scalars(8);
   double cn = hscal_[kNormX];
   if (!(cn > 0.0)) cn = 1.0;
@@ -567,8 +577,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
     DBuf drhs((size_t)nl, s_);
     op.apply_fp64(prev, drhs.p, s_);
     axpby(1.0, rhs.p, -1.0, drhs.p, nl, s_);   // drhs = rhs - B x_prev
-    nrm2(red_, rhs.p, nl, slot(kNormRhs), s_);
-    nrm2(red_, drhs.p, nl, slot(kNormDrhs), s_);
+    nrm2_multi(red_, VecSegs().norm(rhs.p, nl, slot(kNormRhs)).norm(drhs.p, nl, slot(kNormDrhs)), s_);
     read_scalars(2);
     norm_rhs = hscal_[kNormRhs];
     const double nd = hscal_[kNormDrhs];
@@ -577,14 +586,14 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
       const double eps_local = real_tol * norm_rhs / nd;
       GmresResult gr = gmres(op, drhs.p, sol.p, p_.local_iterations, eps_local, p_.resets, gws_, red_, s_);
       st_.gmres_iterations += gr.nit;
+      note_gmres(gr);
       if (p_.prec != kNoPrec) {
         op.apply_prec(sol.p, tmp.p, s_);
         copy(tmp.p, sol.p, nl, s_);
       }
       axpby(1.0, prev, 1.0, sol.p, nl, s_);   // solution_now += previous_solution
       op.apply_fp64(sol.p, tmp.p, s_);
-      sub(tmp.p, rhs.p, tmp.p, nl, s_);
-      nrm2(red_, tmp.p, nl, slot(kResNew), s_);
+      sub_nrm2(red_, tmp.p, rhs.p, tmp.p, nl, slot(kResNew), s_);
       read_scalars(3);
       res_new = hscal_[kResNew] / norm_rhs;
     } else {
@@ -600,6 +609,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
         if (thr < p_.lowp_floor) thr = p_.lowp_floor;
         GmresResult gr = gmres(op, drhs.p, dx.p, p_.local_iterations, thr, p_.resets, gws_, red_, s_);
         st_.gmres_iterations += gr.nit;
+        note_gmres(gr);
         st_.refinements++;
         if (p_.prec != kNoPrec) {
           op.apply_prec(dx.p, tmp.p, s_);
@@ -607,8 +617,7 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
         }
         axpby(1.0, dx.p, 1.0, sol.p, nl, s_);
         op.apply_fp64(sol.p, tmp.p, s_);
-        sub(rhs.p, tmp.p, drhs.p, nl, s_);      // drhs = rhs - B x
-        nrm2(red_, drhs.p, nl, slot(kResNew), s_);
+        sub_nrm2(red_, rhs.p, tmp.p, drhs.p, nl, slot(kResNew), s_);   // drhs = rhs - B x
         read_scalars(3);
         const double nw = hscal_[kResNew];
         const bool stalled = nw > 0.5 * cur;
@@ -723,16 +732,19 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
     // next interfaces (amen_solve.h:482-503)
     phi_A(true, Phis_[k], x_[k].data(), rk, k2, x_[k].data(), rk, k2, k, Phis_[k + 1]);
     phi_b(true, Phis_b_[k], x_[k].data(), rk, k2, k, Phis_b_[k + 1]);
-    nrm2(red_, Phis_[k + 1].data(), Phis_[k + 1].numel(), slot(kNormPhi), s_);
-    nrm2(red_, Phis_b_[k + 1].data(), Phis_b_[k + 1].numel(), slot(kNormPhiB), s_);
-    scale_dev(Phis_[k + 1].data(), Phis_[k + 1].numel(), nullptr, slot(kNormPhi), s_);
-    scale_dev(Phis_b_[k + 1].data(), Phis_b_[k + 1].numel(), nullptr, slot(kNormPhiB), s_);
+    nrm2_multi(red_, VecSegs()
+                           .norm(Phis_[k + 1].data(), Phis_[k + 1].numel(), slot(kNormPhi))
+                           .norm(Phis_b_[k + 1].data(), Phis_b_[k + 1].numel(), slot(kNormPhiB)), s_);
+    VecSegs scl;
+    scl.scale(Phis_[k + 1].data(), Phis_[k + 1].numel(), slot(kNormPhi))
+        .scale(Phis_b_[k + 1].data(), Phis_b_[k + 1].numel(), slot(kNormPhiB));
     if (!last) {
       phi_A(true, Phiz_[k], z_[k].data(), rz_[k], rz_[k + 1], x_[k].data(), rk, k2, k, Phiz_[k + 1]);
       phi_b(true, Phiz_b_[k], z_[k].data(), rz_[k], rz_[k + 1], k, Phiz_b_[k + 1]);
-      scale_dev(Phiz_[k + 1].data(), Phiz_[k + 1].numel(), nullptr, slot(kNormPhi), s_);
-      scale_dev(Phiz_b_[k + 1].data(), Phiz_b_[k + 1].numel(), nullptr, slot(kNormPhiB), s_);
+      scl.scale(Phiz_[k + 1].data(), Phiz_[k + 1].numel(), slot(kNormPhi))
+          .scale(Phiz_b_[k + 1].data(), Phiz_b_[k + 1].numel(), slot(kNormPhiB));
     }
+    scale_multi(scl, s_);
     read_scalars(8);
     double nv = hscal_[kNormV];
     if (!(nv > 0.0)) nv = 1.0;
@@ -1013,7 +1025,8 @@ size_t footprint_bound(const TTView& A, const TTView& b, const TTView& x0, const
   const double local = (double)(p.local_iterations + 1) * nloc + 2.0 * nloc * (double)smax +
                        2.0 * nloc * (double)smax /* split copies, 2 x FP32 */ + 6.0 * nloc +
                        4.0 * r * r + 16.0 * nloc;
-  return (size_t)(8.0 * ((double)A.d * per_core + local)) + ((size_t)64 << 20);
+  // plus the split-K workspace of the solve's stream and 64 MiB for small buffers
+  return (size_t)(8.0 * ((double)A.d * per_core + local)) + split_ws_bytes() + ((size_t)64 << 20);
 }
 
 void randn(double* out, int64_t n, uint64_t seed, uint64_t offset, cudaStream_t s) {

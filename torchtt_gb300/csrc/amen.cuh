@@ -76,6 +76,9 @@ struct AmenStats {
   int64_t krylov_launches = 0;
   double krylov_bytes = 0.0;
   double krylov_traffic_bytes = 0.0;
+  int64_t gmres_syncs = 0;
+  int64_t gmres_overrun = 0;
+  int64_t gmres_reorth = 0;
   // filled when AmenParams::profile is set: CUDA-event time of the contraction launches and the
   // flops of their GEMMs (an A stage run from the nonzeros of a sparse core is not counted)
   double contract_ms = 0.0;

@@ -4,6 +4,7 @@
 #include <mutex>
 
 #include "blas1.cuh"
+#include "reduce.cuh"
 
 namespace ttgb {
 
@@ -25,51 +26,19 @@ void smem_optin(const void* kernel, int bytes) {
 
 namespace {
 
-constexpr int RT = 256;   // threads per reduction block
+using red::RT;
+using red::block_sum;
 constexpr int KC = 8;     // vectors per multi-dot chunk
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// block-wide sum of one value per thread; result valid in thread 0
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-  v = warp_sum(v);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  double r = 0.0;
-  if (w == 0) {
-    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
-    r = warp_sum(r);
-  }
-  __syncthreads();
-  return r;
-}
 
 // Called by every block after writing its partials: the last block sums them in block order.
 // post: 0 = plain sums, 1 = sqrt of vector 0.
 __device__ void last_block_reduce(double* partial, unsigned* counter, int G, int nvec, double* out,
                                   int post) {
-  __shared__ bool is_last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned t = atomicAdd(counter, 1u);
-    is_last = (t == (unsigned)G - 1);
-  }
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
-  for (int v = threadIdx.x; v < nvec; v += blockDim.x) {
-    double s = 0.0;
-    const volatile double* p = partial + (int64_t)v * G;
-    for (int b = 0; b < G; ++b) s += p[b];
+  if (!red::take_last_ticket(counter)) return;
+  red::reduce_vectors(partial, nvec, G, [&](int v, double s) {
     out[v] = (post == 1 && v == 0) ? sqrt(s) : s;
-  }
-  if (threadIdx.x == 0) *counter = 0u;
+  });
+  red::reset_ticket(counter);
 }
 
 __global__ void __launch_bounds__(RT) nrm2_kernel(const double* __restrict__ x, int64_t n,
@@ -172,6 +141,62 @@ __global__ void __launch_bounds__(RT) gs_update_kernel(const double* __restrict_
   last_block_reduce(partial, counter, gridDim.x, nvec, out, 0);
 }
 
+struct SegParams {
+  const double* x[VecSegs::kMax];
+  double* y[VecSegs::kMax];
+  int64_t n[VecSegs::kMax];
+  int64_t chunk[VecSegs::kMax];
+  double* out[VecSegs::kMax];
+  const double* den[VecSegs::kMax];
+  int first_block[VecSegs::kMax + 1];   // blocks of segment i: [first_block[i], first_block[i+1])
+  int count;
+};
+
+__global__ void __launch_bounds__(RT) nrm2_multi_kernel(SegParams p, double* partial,
+                                                         unsigned* counter) {
+  __shared__ double sh[32];
+  int seg = 0;
+  while (seg + 1 < p.count && (int)blockIdx.x >= p.first_block[seg + 1]) ++seg;
+  const int lb = blockIdx.x - p.first_block[seg];
+  const double* x = p.x[seg];
+  const int64_t beg = lb * p.chunk[seg], end = min(p.n[seg], beg + p.chunk[seg]);
+  double s = 0.0;
+  for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
+    const double v = x[i];
+    s = fma(v, v, s);
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (!red::take_last_ticket(counter)) return;
+  {   // warp i sums segment i's partials (lanes over its blocks in order, then a fixed butterfly)
+    const int lane = threadIdx.x & 31, i = threadIdx.x >> 5;
+    if (i < p.count) {
+      const volatile double* q = partial;
+      double t = 0.0;
+      for (int b = p.first_block[i] + lane; b < p.first_block[i + 1]; b += 32) t += q[b];
+      t = red::warp_sum(t);
+      if (lane == 0) *p.out[i] = sqrt(t);
+    }
+  }
+  red::reset_ticket(counter);
+}
+
+__global__ void scale_multi_kernel(SegParams p, int64_t total) {
+  __shared__ double f[VecSegs::kMax];
+  if ((int)threadIdx.x < p.count) {
+    const double d = *p.den[threadIdx.x];
+    f[threadIdx.x] = (d > 0.0) ? 1.0 / d : 1.0;
+  }
+  __syncthreads();
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = t;
+    int seg = 0;
+    while (seg + 1 < p.count && i >= p.n[seg]) { i -= p.n[seg]; ++seg; }
+    p.y[seg][i] *= f[seg];
+  }
+}
+
 __global__ void axpby_kernel(double a, const double* __restrict__ x, double b, double* y, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -183,6 +208,22 @@ __global__ void sub_kernel(const double* __restrict__ x, const double* __restric
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     z[i] = x[i] - y[i];
+}
+
+__global__ void __launch_bounds__(RT) sub_nrm2_kernel(const double* x, const double* y, double* z,
+                                                       int64_t n, int64_t chunk, double* partial,
+                                                       unsigned* counter, double* out) {
+  __shared__ double sh[32];
+  const int64_t beg = blockIdx.x * chunk, end = min(n, beg + chunk);
+  double s = 0.0;
+  for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
+    const double v = x[i] - y[i];
+    z[i] = v;
+    s = fma(v, v, s);
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  last_block_reduce(partial, counter, gridDim.x, 1, out, 1);
 }
 
 __global__ void scale_dev_kernel(double* x, int64_t n, const double* num, const double* den) {
@@ -269,14 +310,14 @@ unsigned ew_grid(int64_t n) {
 }  // namespace
 
 int red_blocks(int64_t n) {
-  int64_t g = (n + 2047) / 2048;
-  const int64_t cap = 2 * (int64_t)num_sms();
+  int64_t g = (n + 511) / 512;
+  const int64_t cap = 4 * (int64_t)num_sms();
   if (g > cap) g = cap;
   if (g < 1) g = 1;
   return (int)g;
 }
 
-static void red_launch_dims(const RedWS& ws, int64_t n, int nvec, int& G, int64_t& chunk) {
+void red_launch_dims(const RedWS& ws, int64_t n, int nvec, int& G, int64_t& chunk) {
   G = red_blocks(n);
   if (G > ws.cap_blocks) G = ws.cap_blocks;
   chunk = (n + G - 1) / G;
@@ -319,6 +360,47 @@ void gs_update(const RedWS& ws, const double* Q, int64_t ldq, int k, const doubl
   TTGB_CHECK_LAUNCH();
 }
 
+void nrm2_multi(const RedWS& ws, const VecSegs& v, cudaStream_t s) {
+  TTGB_REQUIRE(v.count >= 1 && v.count <= VecSegs::kMax, "nrm2_multi: 1 to 4 segments");
+  SegParams p{};
+  p.count = v.count;
+  int G = 0;
+  for (int i = 0; i < v.count; ++i) {
+    int g = red_blocks(v.n[i]);
+    if (g > ws.cap_blocks / v.count) g = ws.cap_blocks / v.count;
+    int64_t chunk = (v.n[i] + g - 1) / g;
+    chunk = ((chunk + 255) / 256) * 256;
+    if (chunk < 256) chunk = 256;
+    g = (int)((v.n[i] + chunk - 1) / chunk);
+    if (g < 1) g = 1;
+    p.x[i] = v.x[i];
+    p.n[i] = v.n[i];
+    p.chunk[i] = chunk;
+    p.out[i] = v.out[i];
+    p.first_block[i] = G;
+    G += g;
+  }
+  p.first_block[v.count] = G;
+  nrm2_multi_kernel<<<G, RT, 0, s>>>(p, ws.partial, ws.counter);
+  TTGB_CHECK_LAUNCH();
+}
+
+void scale_multi(const VecSegs& v, cudaStream_t s) {
+  TTGB_REQUIRE(v.count >= 1 && v.count <= VecSegs::kMax, "scale_multi: 1 to 4 segments");
+  SegParams p{};
+  p.count = v.count;
+  int64_t total = 0;
+  for (int i = 0; i < v.count; ++i) {
+    p.y[i] = v.x[i];
+    p.n[i] = v.n[i];
+    p.den[i] = v.den[i];
+    total += v.n[i];
+  }
+  if (total <= 0) return;
+  scale_multi_kernel<<<ew_grid(total), 256, 0, s>>>(p, total);
+  TTGB_CHECK_LAUNCH();
+}
+
 void axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream_t s) {
   if (n <= 0) return;
   axpby_kernel<<<ew_grid(n), 256, 0, s>>>(a, x, b, y, n);
@@ -328,6 +410,14 @@ void axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream
 void sub(const double* x, const double* y, double* z, int64_t n, cudaStream_t s) {
   if (n <= 0) return;
   sub_kernel<<<ew_grid(n), 256, 0, s>>>(x, y, z, n);
+  TTGB_CHECK_LAUNCH();
+}
+
+void sub_nrm2(const RedWS& ws, const double* x, const double* y, double* z, int64_t n, double* out,
+              cudaStream_t s) {
+  int G; int64_t chunk;
+  red_launch_dims(ws, n, 1, G, chunk);
+  sub_nrm2_kernel<<<G, RT, 0, s>>>(x, y, z, n, chunk, ws.partial, ws.counter, out);
   TTGB_CHECK_LAUNCH();
 }
 

@@ -74,12 +74,12 @@ struct Scratch {   // per-call workspace of the kernel-level entry points
   LinalgWS lws;
   char* hbuf = nullptr;
   explicit Scratch(cudaStream_t st) : s(st) {
-    partial.reset(512 * 128, s);
+    partial.reset(1024 * 128, s);
     TTGB_CUDA(cudaMallocAsync((void**)&counter, 64, s));
     TTGB_CUDA(cudaMemsetAsync(counter, 0, 64, s));
     red.partial = partial.p;
     red.counter = counter;
-    red.cap_blocks = 512;
+    red.cap_blocks = 1024;
     red.cap_vec = 127;
     TTGB_CUDA(cudaMallocAsync((void**)&lws.status, 16, s));
     TTGB_CUDA(cudaMemsetAsync(lws.status, 0, 16, s));
@@ -217,6 +217,9 @@ int ttgb_solution_stats(const ttgb_solution* sol, ttgb_stats* st) {
     st->krylov_launches = a.krylov_launches;
     st->krylov_bytes = a.krylov_bytes;
     st->krylov_traffic_bytes = a.krylov_traffic_bytes;
+    st->gmres_syncs = a.gmres_syncs;
+    st->gmres_overrun = a.gmres_overrun;
+    st->gmres_reorth = a.gmres_reorth;
   });
 }
 
@@ -489,7 +492,7 @@ int ttgb_local_gmres(int64_t r, int64_t s, int64_t n, int64_t S, int64_t R, cons
       op.wp = wp.p;
     }
     GmresWS gws;
-    TTGB_CUDA(cudaMallocAsync((void**)&gws.d_flag, 16, sc.s));
+    TTGB_CUDA(cudaMallocAsync((void**)&gws.d_flag, 32, sc.s));
     gws.h_flag = (int*)(sc.hbuf + 64);
     GmresResult g;
     try {
@@ -553,6 +556,6 @@ int ttgb_pool_usage(int64_t* used_now, int64_t* used_high, int32_t reset_high) {
   });
 }
 
-int32_t ttgb_version(void) { return 102; }
+int32_t ttgb_version(void) { return 103; }
 
 }  // extern "C"

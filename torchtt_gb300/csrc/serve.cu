@@ -17,6 +17,7 @@
 
 #include "../../include/ttgb300.h"
 #include "amen.cuh"
+#include "contract.cuh"
 #include "solution.cuh"
 
 using namespace ttgb;
@@ -127,7 +128,10 @@ struct ttgb_server {
       cv_done.notify_all();
       cv_work.notify_all();
     }
-    if (st) cudaStreamDestroy(st);
+    if (st) {
+      release_split_workspace(st);
+      cudaStreamDestroy(st);
+    }
   }
 };
 

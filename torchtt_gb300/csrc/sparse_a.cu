@@ -19,6 +19,7 @@ sparse_stage_kernel(const int* __restrict__ rp, const int* __restrict__ ja,
                     const T* __restrict__ in, T* out, float* out_lo, StageDims g) {
   __shared__ T sv[SparseCore::kMaxRow];
   __shared__ int64_t soff[SparseCore::kMaxRow];
+  if (g.gate != nullptr && *g.gate != 0) return;
   const int key = blockIdx.x;
   const int beg = rp[key];
   const int cnt = rp[key + 1] - beg;

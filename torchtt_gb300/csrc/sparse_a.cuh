@@ -42,6 +42,7 @@ struct SparseCore {
 struct StageDims {
   int64_t O1, O2, si1, so1, sk, pa, pb;
   int64_t ke0 = 0, sk1 = 0;
+  const int* gate = nullptr;   // device flag: when non-zero at launch time the stage does nothing
 };
 void sparse_stage(const SparseCsr& c, const double* in, double* out, const StageDims& g,
                   cudaStream_t s);

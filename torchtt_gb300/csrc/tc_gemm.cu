@@ -108,12 +108,17 @@ struct TmaParams {
   float* C_lo;
   TcAx cm, cn;
   int64_t c_bs;
+  const int* gate;   // when non-zero at launch time every CTA returns before any set-up
 };
 
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1) tc_gemm_tma_kernel(const __grid_constant__ TmaParams P,
                                                                   int* err) {
   extern __shared__ uint8_t smraw[];
+  // a gated launch (a GMRES iteration queued past its stopping point) leaves before any barrier,
+  // allocation or copy; the flag is set by an earlier kernel on this stream, so every thread of
+  // every CTA reads the same value
+  if (P.gate != nullptr && *P.gate != 0) return;
   uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   constexpr int kABytes = kBM * 128;   // one 128-row operand tile of a chunk (hi or lo)
   constexpr int kBBytes = BN * 128;
@@ -328,6 +333,7 @@ void launch(const TcGemm& g, int* err, cudaStream_t s) {
   P.a_batched = a_b ? 1 : 0;
   P.b_batched = b_b ? 1 : 0;
   P.out = g.out; P.alpha = g.alpha;
+  P.gate = g.gate;
   P.C32 = g.C32; P.C64 = g.C64; P.C_hi = g.C_hi; P.C_lo = g.C_lo;
   P.cm = g.cm; P.cn = g.cn; P.c_bs = g.c_bs;
   constexpr int kStageBytes = 2 * kBM * 128 + 2 * BN * 128;

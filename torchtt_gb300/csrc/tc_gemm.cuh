@@ -39,6 +39,7 @@ struct TcGemm {
   TcAx cm, cn;
   int64_t c_bs = 0;
   float alpha = 1.0f;
+  const int* gate = nullptr;   // device flag: when non-zero at launch time the GEMM does nothing
 };
 
 // Launches the tcgen05 GEMM; `err` (device int) is set non-zero when a bounded wait gave up.

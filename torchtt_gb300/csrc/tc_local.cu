@@ -44,8 +44,8 @@ void TcLocal::setup(const LocalOpDims& dims, const double* phi_l, const double* 
   yh.ensure(ny, st); yl.ensure(ny, st);
 }
 
-void TcLocal::apply(const double* x, double* y, cudaStream_t st) {
-  {   // x^P[(n,R), r] = x[r, n, R], rows of r
+void TcLocal::apply(const double* x, double* y, cudaStream_t st, bool presplit, const int* gate) {
+  if (!presplit) {   // x^P[(n,R), r] = x[r, n, R], rows of r
     Gather4 g;
     g.e0 = d.r; g.s0 = d.n * d.R;
     g.e1 = 1;   g.s1 = 0;
@@ -62,6 +62,7 @@ void TcLocal::apply(const double* x, double* y, cudaStream_t st) {
       t.out = kTcOutF32; t.C32 = wf.p;
       t.cm.e0 = (int)d.R; t.cm.s0 = 1; t.cm.s1 = d.R;                          // row (n, R)
       t.cn.e0 = (int)d.s; t.cn.s0 = d.n * d.R; t.cn.s1 = d.s * d.n * d.R;      // col (l, s)
+      t.gate = gate;
       tc_gemm(t, err, st);
     }
     // Y2[l][m][(S, R)] = sum A[s,m,n,S] W[l][s][n][R], written as the TF32 split with rows (l, m)
@@ -69,6 +70,7 @@ void TcLocal::apply(const double* x, double* y, cudaStream_t st) {
     StageDims g{d.rl, d.R, d.s * d.n * d.R, d.m * ld_SR, d.R, d.n * d.R, d.R};
     g.ke0 = d.S;
     g.sk1 = ld_SR;
+    g.gate = gate;
     sparse_stage_split(sp->lp, wf.p, yh.p, yl.p, g, st);
   } else {
     {   // W[l][R][(s, n)] = x^P[(n,R), r] . Phi_l[(l,s), r], rows (l, R) of pitch ld_sn
@@ -79,6 +81,7 @@ void TcLocal::apply(const double* x, double* y, cudaStream_t st) {
       t.out = kTcOutSplit; t.C_hi = wh.p; t.C_lo = wl.p;
       t.cm.e0 = (int)d.R; t.cm.s1 = 1; t.cm.s0 = ld_sn;                     // row (n, R)
       t.cn.e0 = (int)d.s; t.cn.s1 = d.R * ld_sn; t.cn.s0 = d.n;             // col (l, s)
+      t.gate = gate;
       tc_gemm(t, err, st);
     }
     {   // Y2_l[(m,S), R] = A'[(m,S),(s,n)] . W_l[R, (s,n)]   (batched over l)
@@ -89,6 +92,7 @@ void TcLocal::apply(const double* x, double* y, cudaStream_t st) {
       t.out = kTcOutSplit; t.C_hi = yh.p; t.C_lo = yl.p;
       t.cm.e0 = (int)d.S; t.cm.s1 = ld_SR; t.cm.s0 = d.R;                   // row (m, S)
       t.cn.s0 = 1; t.c_bs = d.m * ld_SR;
+      t.gate = gate;
       tc_gemm(t, err, st);
     }
   }
@@ -99,6 +103,7 @@ void TcLocal::apply(const double* x, double* y, cudaStream_t st) {
     t.B_hi = phr_h.p; t.B_lo = phr_l.p; t.ldb = ld_SR;
     t.out = kTcOutF64; t.C64 = y;
     t.cm.s0 = d.RL; t.cn.s0 = 1;
+    t.gate = gate;
     tc_gemm(t, err, st);
   }
 }

@@ -30,7 +30,11 @@ struct TcLocal {
   int* err = nullptr;   // device flag of the bounded waits
   void setup(const LocalOpDims& dims, const double* phi_l, const double* phi_r, const TcCore* c,
              const SparseCore* spa, int* errflag, cudaStream_t st);
-  void apply(const double* x, double* y, cudaStream_t st);
+  // presplit: xh / xl already hold x's split (written by the producer of x), so the split
+  // launch is skipped. gate (device flag, optional): the GEMMs and the A stage do nothing when
+  // it is non-zero at launch time.
+  void apply(const double* x, double* y, cudaStream_t st, bool presplit = false,
+             const int* gate = nullptr);
 };
 
 }  // namespace ttgb
