@@ -178,6 +178,8 @@ class AmenRun {
     if (phases_) phases_->mark(p);
   }
 
+  static constexpr double kMixedOrthTol = 1e-8;
+
   void note_gmres(const GmresResult& gr) {
     st_.gmres_syncs += gr.syncs;
     st_.host_syncs += gr.syncs;
@@ -607,7 +609,10 @@ void AmenRun::forward_step(int k, int swp, bool last, double& max_res) {
       for (int it = 0; it < p_.max_refine && cur > target; ++it) {
         double thr = target / cur;
         if (thr < p_.lowp_floor) thr = p_.lowp_floor;
-        GmresResult gr = gmres(op, drhs.p, dx.p, p_.local_iterations, thr, p_.resets, gws_, red_, s_);
+        // the correction is solved to thr >= lowp_floor with a low-precision operator: a basis kept
+        // orthogonal to 1e-8 (semi-orthogonality) is far inside that
+        GmresResult gr = gmres(op, drhs.p, dx.p, p_.local_iterations, thr, p_.resets, gws_, red_, s_,
+                               kMixedOrthTol);
         st_.gmres_iterations += gr.nit;
         note_gmres(gr);
         st_.refinements++;
@@ -1025,8 +1030,7 @@ size_t footprint_bound(const TTView& A, const TTView& b, const TTView& x0, const
   const double local = (double)(p.local_iterations + 1) * nloc + 2.0 * nloc * (double)smax +
                        2.0 * nloc * (double)smax /* split copies, 2 x FP32 */ + 6.0 * nloc +
                        4.0 * r * r + 16.0 * nloc;
-  // plus the split-K workspace of the solve's stream and 64 MiB for small buffers
-  return (size_t)(8.0 * ((double)A.d * per_core + local)) + split_ws_bytes() + ((size_t)64 << 20);
+  return (size_t)(8.0 * ((double)A.d * per_core + local)) + ((size_t)64 << 20);
 }
 
 void randn(double* out, int64_t n, uint64_t seed, uint64_t offset, cudaStream_t s) {

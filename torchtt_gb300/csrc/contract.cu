@@ -18,7 +18,6 @@
 #include <shared_mutex>
 #include <type_traits>
 #include <unordered_map>
-#include <mutex>
 
 #include "contract.cuh"
 #include "df.cuh"
@@ -52,48 +51,10 @@ struct KParams {
   int64_t c_bs;
   T alpha, beta;
   int tri;
-  T* part;         // split-K: partial tiles, (tile, split) major, BM x BN each
-  unsigned* cnt;   // split-K: one ticket per output tile, 0 between launches
 };
 
 constexpr int BK = 16;
 constexpr int NT = 256;
-
-// Split-K without atomics: every split of an output tile stores its partial tile, takes a ticket,
-// and the split that takes the last one adds all the partials in split order into `acc` and
-// writes C (returns true only there). The sum, and so the result, is the same whatever order the
-// splits finish in, and C needs no zeroing launch before the splits run.
-template <typename T, int BM, int BN, int TM, int TN>
-__device__ __forceinline__ bool split_fixup(const KParams<T>& p, T (&acc)[TM][TN], int bidx, int ks) {
-  __shared__ bool is_last;
-  const int tid = threadIdx.x, ty = tid / 16, tx = tid % 16;
-  const int64_t tile = ((int64_t)bidx * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-  T* part = p.part + tile * p.splitk * (BM * BN);
-  T* mine = part + (int64_t)ks * (BM * BN);
-#pragma unroll
-  for (int i = 0; i < TM; ++i)
-#pragma unroll
-    for (int j = 0; j < TN; ++j) mine[(ty + 16 * i) * BN + tx + 16 * j] = acc[i][j];
-  __threadfence();
-  __syncthreads();
-  if (tid == 0) is_last = (atomicAdd(p.cnt + tile, 1u) == (unsigned)p.splitk - 1);
-  __syncthreads();
-  if (!is_last) return false;
-  __threadfence();
-#pragma unroll
-  for (int i = 0; i < TM; ++i)
-#pragma unroll
-    for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
-  for (int s = 0; s < p.splitk; ++s) {
-    const volatile T* q = part + (int64_t)s * (BM * BN);
-#pragma unroll
-    for (int i = 0; i < TM; ++i)
-#pragma unroll
-      for (int j = 0; j < TN; ++j) acc[i][j] += q[(ty + 16 * i) * BN + tx + 16 * j];
-  }
-  if (tid == 0) p.cnt[tile] = 0u;
-  return true;
-}
 
 template <typename T, int BM, int BN>
 __global__ void __launch_bounds__(NT) contract_kernel(KParams<T> p) {
@@ -171,7 +132,6 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams<T> p) {
     __syncthreads();
   }
 
-  if (p.splitk > 1 && !split_fixup<T, BM, BN, TM, TN>(p, acc, bidx, ks)) return;
   T* C = p.C + (int64_t)bidx * p.c_bs;
 #pragma unroll
   for (int i = 0; i < TM; ++i) {
@@ -184,7 +144,11 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams<T> p) {
       if (n >= p.N) continue;
       T* c = C + cmo + ax_off(p.cn, n);
       const T v = p.alpha * acc[i][j];
-      *c = (p.beta == T(0)) ? v : fma(p.beta, *c, v);
+      if (p.splitk > 1) {
+        atomicAdd(c, v);
+      } else {
+        *c = (p.beta == T(0)) ? v : fma(p.beta, *c, v);
+      }
     }
   }
 }
@@ -298,12 +262,6 @@ __global__ void __launch_bounds__(NT) contract_df_kernel(KParams<double> p) {
     __syncthreads();
   }
 
-  double acc[TM][TN];
-#pragma unroll
-  for (int i = 0; i < TM; ++i)
-#pragma unroll
-    for (int j = 0; j < TN; ++j) acc[i][j] = (double)ch[i][j] + (double)cl[i][j];
-  if (p.splitk > 1 && !split_fixup<double, BM, BN, TM, TN>(p, acc, bidx, ks)) return;
   double* C = p.C + (int64_t)bidx * p.c_bs;
 #pragma unroll
   for (int i = 0; i < TM; ++i) {
@@ -315,8 +273,9 @@ __global__ void __launch_bounds__(NT) contract_df_kernel(KParams<double> p) {
       const int n = n0 + tx + 16 * j;
       if (n >= p.N) continue;
       double* c = C + cmo + ax_off(p.cn, n);
-      const double v = p.alpha * acc[i][j];
-      *c = (p.beta == 0.0) ? v : fma(p.beta, *c, v);
+      const double v = p.alpha * ((double)ch[i][j] + (double)cl[i][j]);
+      if (p.splitk > 1) atomicAdd(c, v);
+      else *c = (p.beta == 0.0) ? v : fma(p.beta, *c, v);
     }
   }
 }
@@ -428,9 +387,6 @@ bool overlaps(const T* x, int64_t xs, const T* y, int64_t ys) {
   return x < y + ys + 1 && y < x + xs + 1;
 }
 
-// most output tiles x splits of one split-K launch (the size of a stream's split-K workspace)
-int64_t split_tiles_max() { return 4 * (int64_t)num_sms(); }
-
 // CTAs a split-K launch aims at, in multiples of the SM count (TTGB_SPLIT_TARGET, default 2)
 double split_target() {
   static const double v = [] {
@@ -449,68 +405,26 @@ int heuristic_split(const ContractDescT<T>& d, int bm, int bn, int sms, bool for
   int splitk = (int)((target + t - 1) / t);
   const int maxsplit = d.K / 64;
   if (splitk > maxsplit) splitk = maxsplit;
-  if ((int64_t)splitk * t > split_tiles_max()) splitk = (int)(split_tiles_max() / t);
   return splitk < 1 ? 1 : splitk;
-}
-
-// Split-K workspace of one stream: the partial tiles and the per-tile tickets of its split-K
-// launches (kernels of one stream run in order, so one workspace per stream suffices). It is
-// sized once for the largest split-K launch the engine makes, fewer than 4 x SMs tiles of at most
-// 64 x 64 doubles (split_ws_bytes()), and kept until the stream's owner releases it.
-struct SplitWs {
-  void* part = nullptr;
-  unsigned* cnt = nullptr;
-};
-std::mutex g_split_mu;
-std::unordered_map<cudaStream_t, SplitWs> g_split_ws;
-thread_local bool t_no_alloc = false;   // set by NoAllocScope
-
-// The stream's workspace, allocated (stream-ordered) at its first split-K launch; nullptr when it
-// has none and may not allocate one (NoAllocScope, or a stream being captured).
-SplitWs* split_workspace(cudaStream_t st) {
-  std::lock_guard<std::mutex> g(g_split_mu);
-  auto it = g_split_ws.find(st);
-  if (it != g_split_ws.end()) return &it->second;
-  if (t_no_alloc) return nullptr;
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
-    return nullptr;
-  SplitWs w;
-  TTGB_CUDA(cudaMallocAsync(&w.part, split_ws_bytes(), st));
-  const size_t cnt_bytes = (size_t)split_tiles_max() * sizeof(unsigned);
-  cudaError_t e = cudaMallocAsync((void**)&w.cnt, cnt_bytes, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.cnt, 0, cnt_bytes, st);
-  if (e != cudaSuccess) {
-    cudaFreeAsync(w.part, st);
-    if (w.cnt) cudaFreeAsync(w.cnt, st);
-    throw_cuda(e, "split-K workspace", __FILE__, __LINE__);
-  }
-  return &(g_split_ws[st] = w);
 }
 
 template <typename T>
 void launch_tiles(const ContractDescT<T>& d, KParams<T> p, int bm, int bn, int splitk,
                   cudaStream_t stream) {
   int kchunk = d.K;
-  p.part = nullptr;
-  p.cnt = nullptr;
   if (splitk > 1) {
     kchunk = (int)cdiv(cdiv(d.K, splitk), BK) * BK;
     splitk = (int)cdiv(d.K, kchunk);
   }
-  if (splitk > 1) {
-    const int64_t tiles = (int64_t)cdiv(d.N, bn) * cdiv(d.M, bm) * d.batch;
-    SplitWs* w = (tiles * splitk <= split_tiles_max()) ? split_workspace(stream) : nullptr;
-    if (w) {
-      p.part = static_cast<T*>(w->part);
-      p.cnt = w->cnt;
-    } else {   // no workspace for it: the launch runs without split-K
-      splitk = 1;
-      kchunk = d.K;
-    }
-  }
   p.splitk = splitk;
   p.kchunk = kchunk;
+  if (splitk > 1) {
+    int64_t total = (int64_t)d.M * d.N * d.batch;
+    unsigned g = cdiv(total, 256);
+    if (g > 8192) g = 8192;
+    scale_output_kernel<<<g, 256, 0, stream>>>(p.C, p.M, p.N, p.batch, p.cm, p.cn, p.c_bs, p.beta);
+    TTGB_CHECK_LAUNCH();
+  }
   dim3 grid(cdiv(d.N, bn), cdiv(d.M, bm), (unsigned)(d.batch * splitk));
   TTGB_REQUIRE(grid.y < 65536 && grid.z < 65536, "contraction grid too large");
   if constexpr (std::is_same<T, double>::value) {
@@ -664,20 +578,6 @@ int64_t autotune_classes() {
   std::shared_lock<std::shared_mutex> g(g_tune_mu);
   return (int64_t)g_tune_table.size();
 }
-
-size_t split_ws_bytes() { return (size_t)split_tiles_max() * 64 * 64 * sizeof(double); }
-
-void release_split_workspace(cudaStream_t st) {
-  std::lock_guard<std::mutex> g(g_split_mu);
-  auto it = g_split_ws.find(st);
-  if (it == g_split_ws.end()) return;
-  cudaFreeAsync(it->second.part, st);
-  cudaFreeAsync(it->second.cnt, st);
-  g_split_ws.erase(it);
-}
-
-NoAllocScope::NoAllocScope() : prev_(t_no_alloc) { t_no_alloc = true; }
-NoAllocScope::~NoAllocScope() { t_no_alloc = prev_; }
 
 NoTuningScope::NoTuningScope() : prev_(t_no_tuning_runs) { t_no_tuning_runs = true; }
 NoTuningScope::~NoTuningScope() { t_no_tuning_runs = prev_; }

@@ -67,26 +67,9 @@ struct NoTuningScope {
   bool prev_;
 };
 
-// Within this scope the calling thread's contractions allocate no device memory: a split-K launch
-// on a stream without its split-K workspace runs unsplit instead of allocating one.
-struct NoAllocScope {
-  NoAllocScope();
-  ~NoAllocScope();
-  NoAllocScope(const NoAllocScope&) = delete;
-  NoAllocScope& operator=(const NoAllocScope&) = delete;
- private:
-  bool prev_;
-};
-
-// Bytes of one stream's split-K workspace (allocated at the stream's first split-K launch).
-size_t split_ws_bytes();
-// Frees the split-K workspace of `st` (stream-ordered); owners call it before destroying a stream.
-void release_split_workspace(cudaStream_t st);
-
-// Launches the contraction on `stream`. The tile shape and split-K come from the tile autotuner's
-// record for the launch's shape class, or from an occupancy heuristic (deterministic requests
-// never split K). Split-K partial tiles go to the stream's workspace and the last split of each
-// tile adds them in split order, so a launch's result does not depend on the order its CTAs run.
+// Launches the contraction on `stream`. The tile shape and split-K (C pre-scaled by beta, partial
+// sums added atomically) come from the tile autotuner's record for the launch's shape class, or
+// from an occupancy heuristic (deterministic requests never split K).
 void contract(const ContractDesc& d, cudaStream_t stream, bool deterministic = false);
 // The same engine in FP32 (CUDA-core FFMA), for the low-precision local operator.
 void contract(const ContractDescF& d, cudaStream_t stream, bool deterministic = false);

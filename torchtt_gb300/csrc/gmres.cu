@@ -163,6 +163,7 @@ __global__ void __launch_bounds__(RT) arnoldi_project_kernel(const double* __res
                                                               double* h1, double* scal,
                                                               const int* gate) {
   __shared__ double sh[32];
+  __shared__ double shv[(RT / 32) * KC];
   if (*gate != 0) return;   // an iteration queued past the cycle's stopping point
   const int G = gridDim.x;
   const int64_t beg = blockIdx.x * chunk, end = min(n, beg + chunk);
@@ -179,13 +180,7 @@ __global__ void __launch_bounds__(RT) arnoldi_project_kernel(const double* __res
       for (int j = 0; j < KC; ++j)
         if (j < nc) acc[j] = fma(Q[(int64_t)(c0 + j) * ldq + i], qv, acc[j]);
     }
-#pragma unroll
-    for (int j = 0; j < KC; ++j) {
-      if (j < nc) {
-        const double t = block_sum(acc[j], sh);
-        if (threadIdx.x == 0) partial[(int64_t)(c0 + j) * G + blockIdx.x] = t;
-      }
-    }
+    red::block_sums_to_partials<KC>(acc, nc, shv, partial, c0, G);
   }
   ww = block_sum(ww, sh);
   if (threadIdx.x == 0) partial[(int64_t)kv * G + blockIdx.x] = ww;
@@ -213,10 +208,11 @@ __global__ void __launch_bounds__(RT, KB <= 8 ? 2 : 1) arnoldi_reorth_kernel(con
                                                              double* w, int64_t n, int64_t chunk,
                                                              double* partial, unsigned* counter,
                                                              double* h2, double* scal,
-                                                             const int* gate) {
+                                                             const int* gate, double orth_tol2) {
   __shared__ double sh[32];
   __shared__ double hs[kMaxVec];
   __shared__ double sums[kMaxVec + 1];
+  __shared__ double shv[(RT / 32) * (KB > KC ? KB : KC)];
   if (*gate != 0) return;
   const int G = gridDim.x;
   const int64_t beg = blockIdx.x * chunk, end = min(n, beg + chunk);
@@ -243,13 +239,7 @@ __global__ void __launch_bounds__(RT, KB <= 8 ? 2 : 1) arnoldi_reorth_kernel(con
       for (int j = 0; j < KB; ++j)
         if (j < kv) acc[j] = fma(q[j], v, acc[j]);
     }
-#pragma unroll
-    for (int j = 0; j < KB; ++j) {
-      if (j < kv) {
-        const double t = block_sum(acc[j], sh);
-        if (threadIdx.x == 0) partial[(int64_t)j * G + blockIdx.x] = t;
-      }
-    }
+    red::block_sums_to_partials<(KB > 0 ? KB : 1)>(acc, kv, shv, partial, 0, G);
   } else {
     for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
       double v = w[i];
@@ -268,13 +258,7 @@ __global__ void __launch_bounds__(RT, KB <= 8 ? 2 : 1) arnoldi_reorth_kernel(con
         for (int j = 0; j < KC; ++j)
           if (j < nc) acc[j] = fma(Q[(int64_t)(c0 + j) * ldq + i], qv, acc[j]);
       }
-#pragma unroll
-      for (int j = 0; j < KC; ++j) {
-        if (j < nc) {
-          const double t = block_sum(acc[j], sh);
-          if (threadIdx.x == 0) partial[(int64_t)(c0 + j) * G + blockIdx.x] = t;
-        }
-      }
+      red::block_sums_to_partials<KC>(acc, nc, shv, partial, c0, G);
     }
   }
   ss = block_sum(ss, sh);
@@ -290,7 +274,9 @@ __global__ void __launch_bounds__(RT, KB <= 8 ? 2 : 1) arnoldi_reorth_kernel(con
     double b = 0.0;
     for (int j = 0; j < kv; ++j) b = fma(sums[j], sums[j], b);
     double mode, hp, inv;
-    if (!(a < 0.5 * ww)) {                       // includes NaN: the finishing pass reports it
+    // b <= orth_tol^2 a: the new vector's component along the basis, |V^T w'| / |w'|, is already
+    // below the tolerated loss of orthogonality, so the second projection is not needed either
+    if (!(a < 0.5 * ww) || (a > 0.0 && b <= orth_tol2 * a)) {   // NaN: the finishing pass reports it
       mode = 0.0;
       hp = sqrt(a);
       inv = (hp > 0.0) ? 1.0 / hp : 1.0;
@@ -446,15 +432,15 @@ unsigned elem_grid(int64_t n) {
 
 void launch_reorth(int kv, dim3 g, const double* Q, int64_t ldq, const double* h1, double* w,
                    int64_t n, int64_t chunk, const RedWS& red, double* h2, double* scal,
-                   const int* gate, cudaStream_t s) {
+                   const int* gate, double orth_tol2, cudaStream_t s) {
   if (kv <= 4)
-    arnoldi_reorth_kernel<4><<<g, RT, 0, s>>>(Q, ldq, kv, h1, w, n, chunk, red.partial, red.counter, h2, scal, gate);
+    arnoldi_reorth_kernel<4><<<g, RT, 0, s>>>(Q, ldq, kv, h1, w, n, chunk, red.partial, red.counter, h2, scal, gate, orth_tol2);
   else if (kv <= 8)
-    arnoldi_reorth_kernel<8><<<g, RT, 0, s>>>(Q, ldq, kv, h1, w, n, chunk, red.partial, red.counter, h2, scal, gate);
+    arnoldi_reorth_kernel<8><<<g, RT, 0, s>>>(Q, ldq, kv, h1, w, n, chunk, red.partial, red.counter, h2, scal, gate, orth_tol2);
   else if (kv <= 16)
-    arnoldi_reorth_kernel<16><<<g, RT, 0, s>>>(Q, ldq, kv, h1, w, n, chunk, red.partial, red.counter, h2, scal, gate);
+    arnoldi_reorth_kernel<16><<<g, RT, 0, s>>>(Q, ldq, kv, h1, w, n, chunk, red.partial, red.counter, h2, scal, gate, orth_tol2);
   else
-    arnoldi_reorth_kernel<0><<<g, RT, 0, s>>>(Q, ldq, kv, h1, w, n, chunk, red.partial, red.counter, h2, scal, gate);
+    arnoldi_reorth_kernel<0><<<g, RT, 0, s>>>(Q, ldq, kv, h1, w, n, chunk, red.partial, red.counter, h2, scal, gate, orth_tol2);
   TTGB_CHECK_LAUNCH();
 }
 
@@ -473,7 +459,8 @@ static int first_read(const GmresWS& ws, double threshold, int iters) {
 }
 
 GmresResult gmres(const LocalOperator& op, const double* rhs, double* sol, int iters,
-                  double threshold, int resets, GmresWS& ws, const RedWS& red, cudaStream_t s) {
+                  double threshold, int resets, GmresWS& ws, const RedWS& red, cudaStream_t s,
+                  double orth_tol) {
   GmresResult res;
   const int64_t n = op.size();
   TTGB_REQUIRE(iters >= 1, "gmres: local_iterations must be >= 1");
@@ -525,7 +512,8 @@ GmresResult gmres(const LocalOperator& op, const double* rhs, double* sol, int i
       arnoldi_project_kernel<<<G, RT, 0, s>>>(Q, n, kv, w, n, chunk, red.partial, red.counter, h1, scal,
                                               ws.d_flag + kGmresState);
       TTGB_CHECK_LAUNCH();
-      launch_reorth(kv, dim3(G), Q, n, h1, w, n, chunk, red, h2, scal, ws.d_flag + kGmresState, s);
+      launch_reorth(kv, dim3(G), Q, n, h1, w, n, chunk, red, h2, scal, ws.d_flag + kGmresState,
+                    orth_tol * orth_tol, s);
       arnoldi_finish_kernel<<<G, RT, 0, s>>>(Q, n, kv, h1, h2, w, n, chunk, red.partial, red.counter,
                                              scal, k, iters, H, cs, sn, beta, threshold, ws.d_flag,
                                              so);

@@ -117,7 +117,11 @@ struct GmresResult {
 // Gram-Schmidt), normalises, and runs the Givens rotations and the convergence test on the
 // device. The host reads the stop flag only from the iteration where the convergence rate of the
 // previous cycle predicts the stop; iterations queued past the stop leave the solution unchanged.
+// orth_tol > 0 also skips the second projection when the first leaves |V^T w'| <= orth_tol |w'|
+// (measured in the same pass), i.e. it keeps the basis orthogonal to orth_tol instead of to
+// rounding: for GMRES runs whose own tolerance is far above orth_tol.
 GmresResult gmres(const LocalOperator& op, const double* rhs, double* sol, int iters,
-                  double threshold, int resets, GmresWS& ws, const RedWS& red, cudaStream_t s);
+                  double threshold, int resets, GmresWS& ws, const RedWS& red, cudaStream_t s,
+                  double orth_tol = 0.0);
 
 }  // namespace ttgb

@@ -118,6 +118,7 @@ __global__ void __launch_bounds__(512) chol_kernel(double* G, int n, int64_t shi
 // Same shift / identity check semantics as chol_kernel. One block; both n x n factors live in
 // shared memory, so every step is a shared-memory FP64 update plus one barrier.
 constexpr int kCholSmemMax = 112;
+constexpr double kNearIdentity = 1e-9;   // max |G - I| below which the first-order factor is used
 
 __global__ void __launch_bounds__(512) chol_inv_smem_kernel(const double* __restrict__ Gin, int n,
                                                             int64_t shift_rows, int check_identity,
@@ -132,7 +133,7 @@ __global__ void __launch_bounds__(512) chol_inv_smem_kernel(const double* __rest
   for (int t = tid; t < n * n; t += nt) G[(t / n) * ld + (t % n)] = Gin[t];
   if (tid == 0) bad = 0;
   __syncthreads();
-  if (check_identity) {
+  if (shift_rows == 0) {   // the second and third passes: G = I + E with E small
     double mx = 0.0;
     for (int t = tid; t < n * n; t += nt) {
       const int i = t / n, k = t % n;
@@ -140,8 +141,23 @@ __global__ void __launch_bounds__(512) chol_inv_smem_kernel(const double* __rest
       const double v = G[i * ld + k] - (i == k ? 1.0 : 0.0);
       mx = fmax(mx, isfinite(v) ? fabs(v) : 1e300);
     }
-    mx = block_max_d(mx, sh);
-    if (tid == 0 && !(mx <= 0.1)) *status = 2;
+    mx = block_max_d(mx, sh);   // the same value in every thread: the branches below are uniform
+    if (check_identity && tid == 0 && !(mx <= 0.1)) *status = 2;
+    if (mx <= kNearIdentity) {
+      // First-order factor: R = I + U with U the strict upper triangle of E plus half its
+      // diagonal (U + U^T = E), and R^{-1} = I - U. Both are exact to O(n max|E|^2) <= 1.2e-16
+      // for max|E| <= 1e-9 and n <= 112, so the pass costs O(n^2) instead of the factorisation's
+      // n^3 / 3 serial FP64 multiply-adds.
+      for (int t = tid; t < n * n; t += nt) {
+        const int i = t / n, k = t % n;
+        const double e = (k >= i) ? G[i * ld + k] - (i == k ? 1.0 : 0.0) : 0.0;
+        const double u = (k > i) ? e : (k == i ? 0.5 * e : 0.0);
+        const double id = (i == k) ? 1.0 : 0.0;
+        Rout[t] = id + u;
+        Riout[t] = id - u;
+      }
+      return;
+    }
   }
   if (shift_rows > 0) {
     double tr = 0.0;

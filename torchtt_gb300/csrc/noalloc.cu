@@ -100,8 +100,6 @@ extern "C" int ttgb_local_product_noalloc(int64_t rl, int64_t s, int64_t r, int6
   try {
     // no tile-tuning runs here: they time candidates with events and synchronise the host
     ttgb::NoTuningScope no_tuning;
-    // and no split-K workspace: a stream without one runs its contractions unsplit
-    ttgb::NoAllocScope no_alloc;
     for (int32_t i = 0; i < nrhs; ++i)
       ttgb::local_product(d, phi_l, A, phi_r, x + (int64_t)i * r * n * R,
                           y + (int64_t)i * rl * m * RL, base, base + w1, st);

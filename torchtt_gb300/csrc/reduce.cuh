@@ -31,6 +31,29 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return r;
 }
 
+// Block sums of the first nv of N per-thread values with one barrier: each warp reduces its values
+// by shuffles, then thread j < nv adds the warps' results (in warp order) and stores the block's
+// sum at partial[(first + j) * G + blockIdx.x]. sh holds (blockDim.x / 32) * N doubles.
+template <int N>
+__device__ __forceinline__ void block_sums_to_partials(const double (&v)[N], int nv, double* sh,
+                                                       double* partial, int first, int G) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    if (j < nv) {
+      const double t = warp_sum(v[j]);
+      if (lane == 0) sh[warp * N + j] = t;
+    }
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < nv) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += sh[w * N + threadIdx.x];
+    partial[(int64_t)(first + threadIdx.x) * G + blockIdx.x] = s;
+  }
+  __syncthreads();
+}
+
 // Called by every thread of every block after the block's partials are written. Returns true, in
 // all threads of the block, only in the block that took the last ticket; that block then sees the
 // partials of all the others. The caller of the last block resets the counter with reset_ticket().

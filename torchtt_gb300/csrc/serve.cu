@@ -17,7 +17,6 @@
 
 #include "../../include/ttgb300.h"
 #include "amen.cuh"
-#include "contract.cuh"
 #include "solution.cuh"
 
 using namespace ttgb;
@@ -128,10 +127,7 @@ struct ttgb_server {
       cv_done.notify_all();
       cv_work.notify_all();
     }
-    if (st) {
-      release_split_workspace(st);
-      cudaStreamDestroy(st);
-    }
+    if (st) cudaStreamDestroy(st);
   }
 };
 
