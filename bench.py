@@ -308,18 +308,19 @@ def tt_relres_check(A_cores, x_cores, b_cores):
 
 
 def run_configs(args, dev, engine, strict):
-    """The batched and served workloads beside the headline, each on a stated sample of its full
-    definition, mixed and plain FP64 through the same server with the same slots (so their ratio
-    is the same-batching mixed/FP64 speed-up), within a wall budget (``--configs-budget-s``; a
-    stage's FP64 half runs only when the budget left covers ~2.5x its mixed half):
+    """The batched and served workloads beside the headline, mixed and plain FP64 through the same
+    server with the same slots (so their ratio is the same-batching mixed/FP64 speed-up), within a
+    wall budget (``--configs-budget-s``; a stage runs only while the budget lasts):
 
     * parametric diffusion (256 systems A(theta) = sum_k theta_k L_k, d=10, n=32, rhs rank U{1..16},
-      eps 1e-8, nswp 40, kickrank 8): every 8th system (32, rhs ranks across 1-16);
+      eps 1e-8, nswp 40, kickrank 8): all 256 systems mixed; FP64 on every 8th system (32, rhs
+      ranks across 1-16), whose mixed rate is measured in the same run for the ratio;
     * rounding stress (128 solves, d=16, n=32, A = L + C C^T + I, b = a sum of 4 random TTs rounded
-      to 1e-8 before the solve): terms of rank 4 (b of rank 16, nswp 40) - with the full terms of
-      rank 16 the reference's own solve does not converge in 20 sweeps (relres 0.70, ranks <= 161);
+      to 1e-8 before the solve): terms of rank 4 (b of rank 16, nswp 40), 8 solves - with the full
+      terms of rank 16 the reference's own solve does not converge in 20 sweeps (relres 0.70,
+      ranks <= 161);
     * serving trace (10,000 requests, Poisson arrivals, d U{8..24}, n in {16,32,64}, rhs rank
-      U{1..32}, eps in {1e-6,1e-8,1e-10}): the first 8 requests of the seeded trace at 2
+      U{1..32}, eps in {1e-6,1e-8,1e-10}): the first 16 requests of the seeded trace at 2
       requests/s (above capacity, so the replay measures served throughput with queueing).
     Residuals are checked after each timed run (tt_relres_check), outside the timing."""
     import torch
@@ -353,37 +354,48 @@ def run_configs(args, dev, engine, strict):
                 "max_relres_over_eps": max(rr), "relres_pass_frac": sum(1 for v in rr if v <= 1.0) / len(rr),
                 "max_rank": max(max(st["ranks"]) for _, st in res)}
 
-    def pair(systems, full_count, note, arrivals=None):
+    def pair(systems, full_count, note, arrivals=None, sample=None, sample_note=None):
+        """mixed over `systems`; FP64 over `sample` (default: the same systems), and then the
+        mixed rate of that sample too when it differs, so the ratio compares like with like"""
         out = {"sample": note, "full_size": full_count}
         t0 = time.perf_counter()
         out["mixed"] = served(systems, "mixed", arrivals)
         spent = time.perf_counter() - t0
-        out["extrapolated_full_s"] = {"mixed": full_count / out["mixed"]["solves_per_s"]}
-        if left() > 2.5 * spent:
-            out["fp64"] = served(systems, "fp64", arrivals)
-            out["mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
-            out["extrapolated_full_s"]["fp64"] = full_count / out["fp64"]["solves_per_s"]
+        if len(systems) < full_count:
+            out["extrapolated_full_s"] = {"mixed": full_count / out["mixed"]["solves_per_s"]}
+        sub = systems if sample is None else sample
+        if left() > 2.5 * spent * len(sub) / len(systems):
+            out["fp64"] = served(sub, "fp64", None if sample is not None else arrivals)
+            if sample is not None:
+                out["fp64_sample"] = sample_note
+                out["mixed_on_fp64_sample"] = served(sub, "mixed")
+                ref = out["mixed_on_fp64_sample"]["solves_per_s"]
+            else:
+                ref = out["mixed"]["solves_per_s"]
+            out["mixed_over_fp64"] = ref / out["fp64"]["solves_per_s"]
+            out.setdefault("extrapolated_full_s", {})["fp64"] = full_count / out["fp64"]["solves_per_s"]
         else:
             out["fp64"] = "skipped: the configs budget left did not cover it"
         return out
 
     res = {"budget_s": args.configs_budget_s, "server_slots": args.slots, "strict_eps": strict}
-    sysd = [W.parametric_diffusion_d10_n32(i) for i in range(0, 256, 8)]
+    sysd = [W.parametric_diffusion_d10_n32(i) for i in range(256)]
     systems = [(TT([c.to(dev) for c in w["A"]]), TT([c.to(dev) for c in w["b"]]), w["params"]) for w in sysd]
     res["parametric_diffusion_d10_n32"] = pair(
-        systems, 256, "systems 0, 8, .., 248 of the 256 (rhs ranks across 1-16)")
-    if left() > 0.5 * args.configs_budget_s:
+        systems, 256, "all 256 systems", sample=systems[::8],
+        sample_note="systems 0, 8, .., 248 of the 256 (rhs ranks across 1-16)")
+    if left() > 0.35 * args.configs_budget_s:
         systems = []
-        for i in range(4):
+        for i in range(8):
             w = W.rounding_stress(i, term_rank=4, nswp=40)
             A = TT([c.to(dev) for c in w["A"]])
             b = TT([c.to(dev) for c in w["b"]]).round(w["round_b"])   # rounded before the clock
             systems.append((A, b, w["params"]))
         res["rounding_stress_d16_n32"] = pair(
-            systems, 128, "solves 0-3 of 128 with b = 4 rank-4 terms (rank 16) rounded to 1e-8 on "
+            systems, 128, "solves 0-7 of 128 with b = 4 rank-4 terms (rank 16) rounded to 1e-8 on "
                           "the GPU before the timed region, nswp 40")
-    if left() > 0.3 * args.configs_budget_s:
-        trace = W.serving_trace(8, 2.0, 5)
+    if left() > 0.2 * args.configs_budget_s:
+        trace = W.serving_trace(16, 2.0, 5)
         systems, arrivals = [], []
         for t_arr, i in trace:
             w = W.serving_request(i, 5)
@@ -391,7 +403,7 @@ def run_configs(args, dev, engine, strict):
                             w["params"]))
             arrivals.append(t_arr)
         res["serving_trace"] = pair(
-            systems, 10000, "the first 8 requests of the seeded trace (seed 5) at 2 requests/s, "
+            systems, 10000, "the first 16 requests of the seeded trace (seed 5) at 2 requests/s, "
                             "submitted at their arrival times", arrivals)
     res["elapsed_s"] = time.perf_counter() - t_start
     return res
@@ -703,7 +715,7 @@ def main():
     ap.add_argument("--fp64-solves", type=int, default=2)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--configs-budget-s", type=float, default=180.0,
+    ap.add_argument("--configs-budget-s", type=float, default=360.0,
                     help="wall budget of the batched/served workloads block (0: skip it)")
     ap.add_argument("--strict-eps", action="store_true",
                     help="solve every system to a true relres <= eps (strict_eps: AMEn at eps / 4); "

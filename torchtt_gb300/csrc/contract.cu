@@ -105,18 +105,28 @@ __global__ void __launch_bounds__(NT) contract_kernel(KParams<T> p) {
 #pragma unroll
     for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
 
-  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+  // next K tile's operands in registers while the current one is multiplied (same sum order)
+  T ra[BM / A_ROWS_PER_PASS], rb[BN / B_COLS_PER_PASS];
+  auto load_tile = [&](int k0) {
     const int k = k0 + lk;
     const bool kok = k < kend;
     const int64_t a_koff = kok ? ax_off(p.ak, k) : 0;
     const int64_t b_koff = kok ? ax_off(p.bk, k) : 0;
 #pragma unroll
     for (int i = 0; i < BM / A_ROWS_PER_PASS; ++i)
-      As[lk][lr + i * A_ROWS_PER_PASS] = (kok && a_mok[i]) ? __ldg(A + a_moff[i] + a_koff) : T(0);
+      ra[i] = (kok && a_mok[i]) ? __ldg(A + a_moff[i] + a_koff) : T(0);
 #pragma unroll
     for (int i = 0; i < BN / B_COLS_PER_PASS; ++i)
-      Bs[lk][lr + i * B_COLS_PER_PASS] = (kok && b_nok[i]) ? __ldg(B + b_noff[i] + b_koff) : T(0);
+      rb[i] = (kok && b_nok[i]) ? __ldg(B + b_noff[i] + b_koff) : T(0);
+  };
+  if (kbeg < kend) load_tile(kbeg);
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+#pragma unroll
+    for (int i = 0; i < BM / A_ROWS_PER_PASS; ++i) As[lk][lr + i * A_ROWS_PER_PASS] = ra[i];
+#pragma unroll
+    for (int i = 0; i < BN / B_COLS_PER_PASS; ++i) Bs[lk][lr + i * B_COLS_PER_PASS] = rb[i];
     __syncthreads();
+    if (k0 + BK < kend) load_tile(k0 + BK);
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
       T a[TM], b[TN];
@@ -205,26 +215,40 @@ __global__ void __launch_bounds__(NT) contract_df_kernel(KParams<double> p) {
 #pragma unroll
     for (int j = 0; j < TN; ++j) { ch[i][j] = 0.f; cl[i][j] = 0.f; }
 
-  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+  // The operands of the next K tile are loaded into registers while the current tile is
+  // multiplied (the global-load latency overlaps the arithmetic); the order of the sums is the
+  // same as with a load per tile.
+  double ra[BM / ROWS_PER_PASS], rb[BN / ROWS_PER_PASS];
+  auto load_tile = [&](int k0) {
     const int k = k0 + lk;
     const bool kok = k < kend;
     const int64_t a_koff = kok ? ax_off(p.ak, k) : 0;
     const int64_t b_koff = kok ? ax_off(p.bk, k) : 0;
 #pragma unroll
+    for (int i = 0; i < BM / ROWS_PER_PASS; ++i)
+      ra[i] = (kok && a_mok[i]) ? __ldg(A + a_moff[i] + a_koff) : 0.0;
+#pragma unroll
+    for (int i = 0; i < BN / ROWS_PER_PASS; ++i)
+      rb[i] = (kok && b_nok[i]) ? __ldg(B + b_noff[i] + b_koff) : 0.0;
+  };
+  if (kbeg < kend) load_tile(kbeg);
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+#pragma unroll
     for (int i = 0; i < BM / ROWS_PER_PASS; ++i) {
       float h, l;
-      df_split((kok && a_mok[i]) ? __ldg(A + a_moff[i] + a_koff) : 0.0, h, l);
+      df_split(ra[i], h, l);
       Ah[lk][lr + i * ROWS_PER_PASS] = h;
       Al[lk][lr + i * ROWS_PER_PASS] = l;
     }
 #pragma unroll
     for (int i = 0; i < BN / ROWS_PER_PASS; ++i) {
       float h, l;
-      df_split((kok && b_nok[i]) ? __ldg(B + b_noff[i] + b_koff) : 0.0, h, l);
+      df_split(rb[i], h, l);
       Bh[lk][lr + i * ROWS_PER_PASS] = h;
       Bl[lk][lr + i * ROWS_PER_PASS] = l;
     }
     __syncthreads();
+    if (k0 + BK < kend) load_tile(k0 + BK);
 #pragma unroll 4
     for (int kk = 0; kk < BK; ++kk) {
       float ah[TM], al[TM], bh[TN], bl[TN];
