@@ -1029,7 +1029,7 @@ size_t footprint_bound(const TTView& A, const TTView& b, const TTView& x0, const
   const double nloc = core;
   const double local = (double)(p.local_iterations + 1) * nloc + 2.0 * nloc * (double)smax +
                        2.0 * nloc * (double)smax /* split copies, 2 x FP32 */ + 6.0 * nloc +
-                       4.0 * r * r + 16.0 * nloc;
+                       6.0 * r * r + 16.0 * nloc;
   return (size_t)(8.0 * ((double)A.d * per_core + local)) + ((size_t)64 << 20);
 }
 

@@ -442,7 +442,7 @@ void launch_tiles(const ContractDescT<T>& d, KParams<T> p, int bm, int bn, int s
   }
   p.splitk = splitk;
   p.kchunk = kchunk;
-  if (splitk > 1) {
+  if (splitk > 1 && !(d.c_zero && d.beta == T(0))) {
     int64_t total = (int64_t)d.M * d.N * d.batch;
     unsigned g = cdiv(total, 256);
     if (g > 8192) g = 8192;
@@ -552,6 +552,9 @@ int tuned_choice(const ContractDescT<T>& d, const KParams<T>& p, cudaStream_t st
 template <typename T>
 void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool deterministic) {
   if (d.M <= 0 || d.N <= 0 || d.batch <= 0) return;
+  // the tuning runs write C before the chosen tile runs again: those launches may not assume C = 0
+  ContractDescT<T> dz = d;
+  dz.c_zero = false;
   KParams<T> p;
   p.M = d.M; p.N = d.N; p.K = d.K; p.batch = d.batch;
   p.A = d.A; p.am = to_dev(d.am, d.M); p.ak = to_dev(d.ak, d.K); p.a_bs = d.a_bs;
@@ -568,13 +571,13 @@ void launch_contract(const ContractDescT<T>& d, cudaStream_t stream, bool determ
   const int sms = num_sms();
   if (!deterministic && autotune_on()) {
     bool tuned = false;
-    const int c = tuned_choice(d, p, stream, tuned);
+    const int c = tuned_choice(dz, p, stream, tuned);
     // after tuning, C holds the last candidate's result: the chosen tile runs once more, so the
     // first launch of a class gives what every later launch of the class computes
     if (c >= 0) {
       const TileCfg& t = kCandidates[c];
-      launch_tiles(d, p, t.bm, t.bn, t.split ? heuristic_split(d, t.bm, t.bn, sms, true) : 1,
-                   stream);
+      launch_tiles(tuned ? dz : d, p, t.bm, t.bn,
+                   t.split ? heuristic_split(d, t.bm, t.bn, sms, true) : 1, stream);
       return;
     }
   }

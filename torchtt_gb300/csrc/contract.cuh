@@ -36,6 +36,9 @@ struct ContractDescT {
   // product whose upper part is not read); kTriUpperB treats B(k, n) as zero for k > n (an upper
   // triangular right factor), so a column tile sums only k < its last column.
   int tri = 0;
+  // C holds zeros on entry (with beta = 0): a split-K launch then adds its partial sums into C
+  // without the launch that would first scale C by beta
+  bool c_zero = false;
 };
 constexpr int kTriLowerC = 1;
 constexpr int kTriUpperB = 2;

@@ -1,6 +1,7 @@
 // Restarted GMRES on the local AMEn operator, with the Krylov basis, the Hessenberg matrix, the
 // Givens rotations and the convergence test kept on the device (reference: cpp/gmres.h:34-161).
-// The host reads one 8-byte flag per iteration to stop; everything else stays device resident.
+// The host reads the stop flag only from the iteration where the previous cycle's convergence rate
+// predicts the stop; everything else stays device resident.
 #include <cmath>
 
 #include "gmres.cuh"

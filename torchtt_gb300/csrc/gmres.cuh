@@ -66,7 +66,8 @@ struct LocalOperator {
   Profiler* prof_lowp = nullptr;  // optional timing of the low-precision products
   // optional timing of the Krylov orthogonalisation of each GMRES iteration; its first figure is
   // the reference's algorithmic bytes 8 N_loc (2k + 3) of iteration k (k + 1 basis vectors), the
-  // second the bytes the CGS2 kernels read and write, 8 N_loc (4k + 10)
+  // second the bytes the Arnoldi kernels read and write, 8 N_loc (2k + 7), plus 8 N_loc (k + 1)
+  // for an iteration that takes the second projection
   Profiler* prof_krylov = nullptr;
   int64_t* count_lowp = nullptr;
   int64_t size() const { return dims.r * dims.n * dims.R; }

@@ -120,7 +120,9 @@ __global__ void __launch_bounds__(512) chol_kernel(double* G, int n, int64_t shi
 constexpr int kCholSmemMax = 112;
 constexpr double kNearIdentity = 1e-9;   // max |G - I| below which the first-order factor is used
 
-__global__ void __launch_bounds__(512) chol_inv_smem_kernel(const double* __restrict__ Gin, int n,
+// Gin is cleared after it is read (the next Gram product accumulates into it); Rout and Riout
+// must not overlap it.
+__global__ void __launch_bounds__(512) chol_inv_smem_kernel(double* __restrict__ Gin, int n,
                                                             int64_t shift_rows, int check_identity,
                                                             double* Rout, double* Riout, int* status) {
   extern __shared__ double sm[];
@@ -133,6 +135,7 @@ __global__ void __launch_bounds__(512) chol_inv_smem_kernel(const double* __rest
   for (int t = tid; t < n * n; t += nt) G[(t / n) * ld + (t % n)] = Gin[t];
   if (tid == 0) bad = 0;
   __syncthreads();
+  for (int t = tid; t < n * n; t += nt) Gin[t] = 0.0;   // ready for the next Gram product
   if (shift_rows == 0) {   // the second and third passes: G = I + E with E small
     double mx = 0.0;
     for (int t = tid; t < n * n; t += nt) {
@@ -1025,7 +1028,7 @@ void qr_r(const double* A, int64_t lda, int64_t m, int64_t n, double* R, LinalgW
 
 void gemm_cm(const double* A, int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
              int64_t m, int64_t n, int64_t k, double alpha, double beta, cudaStream_t s,
-             bool transA, bool transB, int tri) {
+             bool transA, bool transB, int tri, bool c_zero) {
   ContractDesc c;
   c.M = (int)m; c.N = (int)n; c.K = (int)k;
   c.A = A;
@@ -1037,6 +1040,7 @@ void gemm_cm(const double* A, int64_t lda, const double* B, int64_t ldb, double*
   c.C = C; c.cm = Ax::one(1); c.cn = Ax::one(ldc);
   c.alpha = alpha; c.beta = beta;
   c.tri = tri;
+  c.c_zero = c_zero;
   contract(c, s);
 }
 
@@ -1055,41 +1059,46 @@ QRResult qr(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, doubl
     return res;
   }
   // shifted CholeskyQR3
-  ws.a.ensure(4 * n * n + 16, s);
-  double* G = ws.a.p;           // n x n Gram / Cholesky factor (row-major R)
-  double* Ri = G + n * n;       // inverse of the current factor
-  double* Rt = Ri + n * n;      // accumulated R (row-major)
-  double* Tm = Rt + n * n;      // temporary
+  ws.a.ensure(5 * n * n + 16, s);
+  double* Rp[3] = {ws.a.p, ws.a.p + n * n, ws.a.p + 2 * n * n};   // R of each pass (row-major)
+  double* Ri = ws.a.p + 3 * n * n;   // inverse of the current factor
+  double* T1 = ws.a.p + 4 * n * n;   // R_1 R_0
+  if (ws.gram.p == nullptr || ws.gram.n < (size_t)(n * n)) {   // (re)allocated: clear it once
+    ws.gram.ensure((size_t)(n * n), s);
+    TTGB_CUDA(cudaMemsetAsync(ws.gram.p, 0, ws.gram.n * sizeof(double), s));
+    ws.gram_zero = (int64_t)ws.gram.n;
+  }
+  double* G = ws.gram.p;             // n x n Gram matrix (row-major upper triangle)
   ws.b.ensure(m * n + 16, s);
   double* Qt = ws.b.p;
   TTGB_CUDA(cudaMemsetAsync(ws.status, 0, sizeof(int), s));
   const double* Ain = A;
   int64_t ldin = lda;
   double* outs[3] = {Q, Qt, Q};
+  const bool smem_chol = n <= kCholSmemMax;
   for (int pass = 0; pass < 3; ++pass) {
-    // Gram matrix: only its lower (column-major) = upper (row-major) triangle is formed and read
-    gemm_cm(Ain, ldin, Ain, ldin, G, n, n, n, m, 1.0, 0.0, s, true, false, kTriLowerC);
-    if (n <= kCholSmemMax) {
+    // Gram matrix: only its lower (column-major) = upper (row-major) triangle is formed and read;
+    // with the shared-memory Cholesky the buffer is already zero (cleared by the previous one)
+    gemm_cm(Ain, ldin, Ain, ldin, G, n, n, n, m, 1.0, 0.0, s, true, false, kTriLowerC,
+            smem_chol && ws.gram_zero >= n * n);
+    if (smem_chol) {
       const size_t smem = (size_t)2 * n * (n + 1) * sizeof(double);
       smem_optin((const void*)chol_inv_smem_kernel,
                  (int)(2 * kCholSmemMax * (kCholSmemMax + 1) * sizeof(double)));
-      chol_inv_smem_kernel<<<1, 512, smem, s>>>(G, (int)n, pass == 0 ? m : 0, pass == 2 ? 1 : 0, G,
-                                                Ri, ws.status);
+      chol_inv_smem_kernel<<<1, 512, smem, s>>>(G, (int)n, pass == 0 ? m : 0, pass == 2 ? 1 : 0,
+                                                Rp[pass], Ri, ws.status);
       TTGB_CHECK_LAUNCH();
+      if (ws.gram_zero < n * n) ws.gram_zero = n * n;   // the kernel cleared [0, n^2)
     } else {
       chol_kernel<<<1, 512, 0, s>>>(G, (int)n, pass == 0 ? m : 0, pass == 2 ? 1 : 0, ws.status);
       TTGB_CHECK_LAUNCH();
       trinv_kernel<<<cdiv(n, 128), 128, 0, s>>>(G, Ri, (int)n);
       TTGB_CHECK_LAUNCH();
+      copy(G, Rp[pass], n * n, s);
+      ws.gram_zero = 0;   // G now holds R
     }
     // Q_next = Ain * R^{-1}   (Ri row-major == (Ri)^T column-major; R^{-1} upper triangular)
     gemm_cm(Ain, ldin, Ri, n, outs[pass], m, m, n, n, 1.0, 0.0, s, false, true, kTriUpperB);
-    if (pass == 0) {
-      copy(G, Rt, n * n, s);
-    } else {  // Rt <- R_pass * Rt  (row-major products via column-major transposes)
-      gemm_cm(Rt, n, G, n, Tm, n, n, n, n, 1.0, 0.0, s, false, false);
-      copy(Tm, Rt, n * n, s);
-    }
     Ain = outs[pass];
     ldin = m;
   }
@@ -1099,8 +1108,10 @@ QRResult qr(const double* A, int64_t lda, int64_t m, int64_t n, double* Q, doubl
     householder(A, lda, m, n, Q, R, ws, s);
     return res;
   }
-  // R (n x n col-major, ld n) from the row-major Rt
-  transpose(Rt, n, R, n, n, n, s);
+  // R = R_2 R_1 R_0 (row-major factors; a row-major X is the column-major X^T):
+  // T1 (row-major) = R_1 R_0, and R (column-major, ld n) = R_2 T1 written directly
+  gemm_cm(Rp[0], n, Rp[1], n, T1, n, n, n, n, 1.0, 0.0, s, false, false);
+  gemm_cm(Rp[2], n, T1, n, R, n, n, n, n, 1.0, 0.0, s, true, true);
   return res;
 }
 

@@ -13,6 +13,11 @@ struct LinalgWS {
   DBuf a, b, c, d, e;
   int* status = nullptr;      // device status word of the last factorisation (0 = ok)
   int* h_status = nullptr;    // pinned host mirror
+  // Gram matrices of CholeskyQR3. The shared-memory Cholesky kernel clears the Gram matrix it has
+  // read, so the next Gram product (split-K, atomic partial sums) starts from zeros without a
+  // zeroing launch; the first gram_zero elements are known to be zero.
+  DBuf gram;
+  int64_t gram_zero = 0;
 };
 
 struct QRResult {
@@ -50,6 +55,6 @@ void gemv(const double* B, int64_t n, const double* x, double* y, cudaStream_t s
 // `tri`: structure flags of the contraction engine (kTriLowerC, kTriUpperB)
 void gemm_cm(const double* A, int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
              int64_t m, int64_t n, int64_t k, double alpha, double beta, cudaStream_t s,
-             bool transA = false, bool transB = false, int tri = 0);
+             bool transA = false, bool transB = false, int tri = 0, bool c_zero = false);
 
 }  // namespace ttgb
