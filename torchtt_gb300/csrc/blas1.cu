@@ -28,7 +28,6 @@ namespace {
 
 using red::RT;
 using red::block_sum;
-constexpr int KC = 8;     // vectors per multi-dot chunk
 
 // Called by every block after writing its partials: the last block sums them in block order.
 // post: 0 = plain sums, 1 = sqrt of vector 0.
@@ -54,91 +53,6 @@ __global__ void __launch_bounds__(RT) nrm2_kernel(const double* __restrict__ x, 
   s = block_sum(s, sh);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
   last_block_reduce(partial, counter, gridDim.x, 1, out, post);
-}
-
-__global__ void __launch_bounds__(RT) dot_kernel(const double* __restrict__ x,
-                                                  const double* __restrict__ y, int64_t n,
-                                                  int64_t chunk, double* partial, unsigned* counter,
-                                                  double* out) {
-  __shared__ double sh[32];
-  const int64_t beg = blockIdx.x * chunk, end = min(n, beg + chunk);
-  double s = 0.0;
-  for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) s = fma(x[i], y[i], s);
-  s = block_sum(s, sh);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s;
-  last_block_reduce(partial, counter, gridDim.x, 1, out, 0);
-}
-
-// partial dots of Q_i . q over this block's element range, for all i < k
-__device__ void block_multidot(const double* __restrict__ Q, int64_t ldq, int k,
-                               const double* q, int64_t beg, int64_t end, double* partial, int G,
-                               double* sh) {
-  for (int c0 = 0; c0 < k; c0 += KC) {
-    double acc[KC];
-#pragma unroll
-    for (int j = 0; j < KC; ++j) acc[j] = 0.0;
-    const int nc = min(KC, k - c0);
-    for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
-      const double qv = q[i];
-#pragma unroll
-      for (int j = 0; j < KC; ++j)
-        if (j < nc) acc[j] = fma(Q[(int64_t)(c0 + j) * ldq + i], qv, acc[j]);
-    }
-#pragma unroll
-    for (int j = 0; j < KC; ++j) {
-      if (j < nc) {
-        const double s = block_sum(acc[j], sh);
-        if (threadIdx.x == 0) partial[(int64_t)(c0 + j) * G + blockIdx.x] = s;
-      }
-    }
-  }
-}
-
-__global__ void __launch_bounds__(RT) multidot_kernel(const double* __restrict__ Q, int64_t ldq,
-                                                       int k, const double* __restrict__ q,
-                                                       int64_t n, int64_t chunk, double* partial,
-                                                       unsigned* counter, double* out) {
-  __shared__ double sh[32];
-  const int64_t beg = blockIdx.x * chunk, end = min(n, beg + chunk);
-  block_multidot(Q, ldq, k, q, beg, end, partial, gridDim.x, sh);
-  last_block_reduce(partial, counter, gridDim.x, k, out, 0);
-}
-
-__global__ void __launch_bounds__(RT) gs_update_kernel(const double* __restrict__ Q, int64_t ldq,
-                                                        int k, const double* __restrict__ h,
-                                                        double* q, int64_t n, int64_t chunk,
-                                                        double* partial, unsigned* counter,
-                                                        double* out, int dots, int sq) {
-  __shared__ double sh[32];
-  __shared__ double hs[256];
-  const int64_t beg = blockIdx.x * chunk, end = min(n, beg + chunk);
-  double ss = 0.0;
-  for (int c0 = 0; c0 < k || (c0 == 0 && k == 0); c0 += 256) {
-    const int nc = min(256, k - c0);
-    __syncthreads();
-    for (int j = threadIdx.x; j < nc; j += blockDim.x) hs[j] = h[c0 + j];
-    __syncthreads();
-    const bool lastc = c0 + 256 >= k;
-    for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
-      double v = q[i];
-      for (int j = 0; j < nc; ++j) v = fma(-hs[j], Q[(int64_t)(c0 + j) * ldq + i], v);
-      q[i] = v;
-      if (lastc) ss = fma(v, v, ss);
-    }
-    if (k == 0) break;
-  }
-  int nvec = 0;
-  if (dots) {
-    __syncthreads();
-    block_multidot(Q, ldq, k, q, beg, end, partial, gridDim.x, sh);
-    nvec = k;
-  }
-  if (sq) {
-    ss = block_sum(ss, sh);
-    if (threadIdx.x == 0) partial[(int64_t)nvec * gridDim.x + blockIdx.x] = ss;
-    nvec += 1;
-  }
-  last_block_reduce(partial, counter, gridDim.x, nvec, out, 0);
 }
 
 struct SegParams {
@@ -280,25 +194,6 @@ __global__ void transpose_kernel(const double* __restrict__ src, int64_t sld, do
   }
 }
 
-__global__ void combine_kernel(const double* __restrict__ Q, int64_t ldq, int k,
-                               const double* __restrict__ c, const double* y0, double* y,
-                               int64_t n) {
-  __shared__ double cs[256];
-  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = i0 + threadIdx.x;
-    double v = (y0 && i < n) ? y0[i] : 0.0;
-    for (int c0 = 0; c0 < k; c0 += 256) {
-      const int nc = min(256, k - c0);
-      __syncthreads();
-      for (int j = threadIdx.x; j < nc; j += blockDim.x) cs[j] = c[c0 + j];
-      __syncthreads();
-      if (i < n)
-        for (int j = 0; j < nc; ++j) v = fma(cs[j], Q[(int64_t)(c0 + j) * ldq + i], v);
-    }
-    if (i < n) y[i] = v;
-  }
-}
-
 unsigned ew_grid(int64_t n) {
   unsigned g = cdiv(n, 256);
   const unsigned cap = (unsigned)num_sms() * 8;
@@ -332,31 +227,6 @@ void nrm2(const RedWS& ws, const double* x, int64_t n, double* out, cudaStream_t
   int G; int64_t chunk;
   red_launch_dims(ws, n, 1, G, chunk);
   nrm2_kernel<<<G, RT, 0, s>>>(x, n, chunk, ws.partial, ws.counter, out, 1);
-  TTGB_CHECK_LAUNCH();
-}
-
-void dot(const RedWS& ws, const double* x, const double* y, int64_t n, double* out, cudaStream_t s) {
-  int G; int64_t chunk;
-  red_launch_dims(ws, n, 1, G, chunk);
-  dot_kernel<<<G, RT, 0, s>>>(x, y, n, chunk, ws.partial, ws.counter, out);
-  TTGB_CHECK_LAUNCH();
-}
-
-void multidot(const RedWS& ws, const double* Q, int64_t ldq, int k, const double* q, int64_t n,
-              double* out, cudaStream_t s) {
-  if (k <= 0) return;
-  int G; int64_t chunk;
-  red_launch_dims(ws, n, k, G, chunk);
-  multidot_kernel<<<G, RT, 0, s>>>(Q, ldq, k, q, n, chunk, ws.partial, ws.counter, out);
-  TTGB_CHECK_LAUNCH();
-}
-
-void gs_update(const RedWS& ws, const double* Q, int64_t ldq, int k, const double* h, double* q,
-               int64_t n, double* out, bool dots, bool sq, cudaStream_t s) {
-  int G; int64_t chunk;
-  red_launch_dims(ws, n, (dots ? k : 0) + (sq ? 1 : 0), G, chunk);
-  gs_update_kernel<<<G, RT, 0, s>>>(Q, ldq, k, h, q, n, chunk, ws.partial, ws.counter, out,
-                                    dots ? 1 : 0, sq ? 1 : 0);
   TTGB_CHECK_LAUNCH();
 }
 
@@ -488,13 +358,6 @@ void scale_rows_cm(double* X, int64_t ld, int64_t rows, int64_t cols, const doub
                    cudaStream_t s) {
   if (rows <= 0 || cols <= 0) return;
   scale_rows_cm_kernel<<<ew_grid(rows * cols), 256, 0, s>>>(X, ld, rows, cols, S);
-  TTGB_CHECK_LAUNCH();
-}
-
-void combine(const double* Q, int64_t ldq, int k, const double* c, const double* y0, double* y,
-             int64_t n, cudaStream_t s) {
-  if (n <= 0) return;
-  combine_kernel<<<ew_grid(n), 256, 0, s>>>(Q, ldq, k, c, y0, y, n);
   TTGB_CHECK_LAUNCH();
 }
 

@@ -22,14 +22,6 @@ void red_launch_dims(const RedWS& ws, int64_t n, int nvec, int& G, int64_t& chun
 
 // out[0] = ||x||_2 (out[1] = ||x||_2^2 if `both`)
 void nrm2(const RedWS& ws, const double* x, int64_t n, double* out, cudaStream_t s);
-// out[0] = x . y
-void dot(const RedWS& ws, const double* x, const double* y, int64_t n, double* out, cudaStream_t s);
-// out[i] = Q_i . q for i < k; Q_i = Q + i*ldq
-void multidot(const RedWS& ws, const double* Q, int64_t ldq, int k, const double* q, int64_t n,
-              double* out, cudaStream_t s);
-// q <- q - sum_i h[i] Q_i; then, if `dots`, out[i] = Q_i . q (i < k); if `sq`, out[0] = ||q||^2
-void gs_update(const RedWS& ws, const double* Q, int64_t ldq, int k, const double* h, double* q,
-               int64_t n, double* out, bool dots, bool sq, cudaStream_t s);
 
 // Up to four vectors handled by one launch: x_i of n_i elements, with a device output (norms) or
 // divisor (scaling) each.
@@ -79,8 +71,5 @@ void scale_rows_cm(double* X, int64_t ld, int64_t rows, int64_t cols, const doub
 // precision casts
 void cast(const double* x, float* y, int64_t n, cudaStream_t s);
 void cast(const float* x, double* y, int64_t n, cudaStream_t s);
-// y = sum_i c[i] * Q_i (+ y0 if y0 != null), c device, Q_i = Q + i*ldq
-void combine(const double* Q, int64_t ldq, int k, const double* c, const double* y0, double* y,
-             int64_t n, cudaStream_t s);
 
 }  // namespace ttgb
