@@ -449,8 +449,9 @@ void launch_reorth(int kv, dim3 g, const double* Q, int64_t ldq, const double* h
 
 // Iterations of a cycle before its first flag read: the convergence rate of the last converged
 // cycle, log(threshold) / iterations, predicts how many this threshold needs; the first read comes
-// one iteration before that (later reads follow every iteration), so an early stop costs at most
-// a rarely queued extra iteration, and a late one an extra read.
+// one iteration before that, and later reads follow every iteration. A stop earlier than predicted
+// leaves the iterations queued after it, whose kernels read the flag and return at once; a later
+// stop costs one more read per extra iteration.
 static int first_read(const GmresWS& ws, double threshold, int iters) {
   if (!(ws.log_rate < 0.0) || !(threshold > 0.0) || !(threshold < 1.0)) return 1;
   const double need = std::log(threshold) / ws.log_rate;
